@@ -1,0 +1,125 @@
+/*
+ * C ABI of the GB300 interval branch-and-bound engine (libsid.so).
+ *
+ * The reference has no foreign-function boundary: its lemma programs call the
+ * C++ template ivarp::run_prover (ivarp/include/ivarp/run_prover.hpp:57-88),
+ * which runs the proof driver (prover/proof_driver.hpp:218-627) with a prover
+ * core (cpu_prover/cpu_prover_core.hpp:31-260 or
+ * with_cuda/ivarp_cuda/gpu_prover_core.cuh:199-470). Here that driver and core
+ * are replaced by this C ABI; the C++ run_prover in include/ivarp/run_prover.hpp
+ * is its only caller on the proof path. Each entry point below names the
+ * reference interface whose job it takes over.
+ *
+ * Conventions: every function returns SID_OK (0) or a negative status; no
+ * exception crosses the boundary; buffers are caller-owned host memory unless
+ * the name ends in _device; an engine handle must not be used from two host
+ * threads at once. All device-side waits are bounded and report
+ * SID_ERR_TIMEOUT instead of hanging.
+ */
+#ifndef SID_H
+#define SID_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SID_OK 0
+#define SID_ERR_INVALID (-1)      /* bad argument or malformed lemma IR */
+#define SID_ERR_CUDA (-2)         /* a CUDA call failed; see sid_last_error() */
+#define SID_ERR_NOT_COMPILED (-3) /* no GPU kernels were built for this lemma IR */
+#define SID_ERR_NOMEM (-4)        /* device allocation failed */
+#define SID_ERR_TIMEOUT (-5)      /* a bounded device wait gave up */
+#define SID_ERR_UNSUPPORTED (-6)  /* setting or feature not supported */
+#define SID_ERR_CAPACITY (-7)     /* result larger than the caller's buffer */
+
+typedef struct sid_engine sid_engine;
+
+/* Proof statistics; field meaning as ivarp::ProofInformation (prover/proof_information.hpp:32-44). */
+typedef struct sid_result {
+    uint64_t num_cuboids;
+    uint64_t num_leaf_cuboids;
+    uint64_t num_critical_cuboids;
+    uint64_t num_repeated_nodes;
+    uint64_t criticals_stored;   /* criticals retained for sid_fetch_criticals */
+    uint64_t escalated;          /* cuboids re-evaluated in FP64 (precision form only) */
+    double seconds;              /* device wall time of the proof */
+} sid_result;
+
+/* Snapshot handed to a progress callback (ivarp::ProgressInfo, default_progress_observer.hpp:30-35). */
+typedef struct sid_progress {
+    uint64_t queue_size;
+    uint64_t cuboid_count;
+    uint64_t leaf_count;
+    uint64_t critical_count;
+    const double* queue_head;    /* 2*nargs doubles (lo,hi per variable) of one queued element, or NULL */
+} sid_progress;
+
+typedef void (*sid_progress_fn)(void* user, const sid_progress* progress);
+
+#define SID_PRECISION_PLAIN 0           /* the lemma's own number type, bit-exact with the reference */
+#define SID_PRECISION_FP32_ESCALATE 1   /* FP32 first pass, undecided cuboids re-checked in FP64 */
+
+/* Settings of one proof; meaning as ivarp::ProverSettings (prover_input.hpp:124-159). */
+typedef struct sid_prove_opts {
+    uint32_t generation_count;          /* default 8 */
+    int32_t max_iterations_per_node;    /* <= 1: no re-iteration (the published proofs use 1) */
+    float iteration_volume_criterion;
+    float iteration_single_dimension_criterion;
+    int64_t batch_elements;             /* queue elements expanded per step; <= 0: engine default */
+    int32_t precision;                  /* SID_PRECISION_* */
+    uint64_t max_criticals_kept;        /* criticals stored for sid_fetch_criticals */
+    sid_progress_fn progress;           /* optional, called from the calling thread between steps */
+    void* progress_user;
+    uint32_t progress_first_ms;         /* delay before the first callback */
+    uint32_t progress_every_ms;
+} sid_prove_opts;
+
+/* Fill `opts` with the defaults above. */
+void sid_prove_opts_default(sid_prove_opts* opts);
+
+/* Human-readable description of the last error on this thread. */
+const char* sid_last_error(void);
+
+/* Create an engine on CUDA device `device` (replaces the device discovery and per-device driver
+ * threads of with_cuda/ivarp_cuda/gpu_prover_core.cuh:237-251). */
+int sid_engine_create(int device, sid_engine** out);
+void sid_engine_destroy(sid_engine* engine);
+
+/* Register a compiled lemma (the text IR written by the front end for an ivarp::ProverInput,
+ * prover_input.hpp:118-122). The engine selects the kernels generated for this IR at build time. */
+int sid_lemma_register(sid_engine* engine, const char* ir, size_t ir_len, int* lemma_id);
+int sid_lemma_info(sid_engine* engine, int lemma_id, int* nargs, uint64_t* fingerprint);
+
+/* Initial runtime box: compile-time bounds tightened by 50*nargs rounds of all bounds
+ * (refactor_constraints_impl.hpp:90-101). out_lohi: 2*nargs doubles. */
+int sid_lemma_root_box(sid_engine* engine, int lemma_id, double* out_lohi);
+
+/* Run a whole proof (ProofDriver::run, proof_driver.hpp:472-489). Returns SID_OK whether or not
+ * criticals remain; the verdict is result->num_critical_cuboids == 0. */
+int sid_prove(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, sid_result* result);
+
+/* Copy the criticals retained by the last sid_prove of this lemma: n*2*nargs doubles, per critical
+ * the (lo,hi) pairs of all variables (the on_critical calls of cpu_prover_core.hpp:137-149). */
+int sid_fetch_criticals(sid_engine* engine, int lemma_id, double* out, uint64_t capacity, uint64_t* n_out);
+
+/* Leaf evaluation of a batch of cuboids: for each cuboid, propagate the bounds after a change of the
+ * last variable (it_limit = nargs, rec_limit = 4) and test all constraints -- the innermost step of
+ * CPUProverCore::p_handle_cuboid (cpu_prover_core.hpp:221-256). Boxes are structure-of-arrays:
+ * lo[v*n + i], hi[v*n + i]. Outputs the propagated box and a verdict per cuboid:
+ * 0 = survives (critical at this level), 1 = empty after propagation, 2 = a constraint is violated.
+ * Host buffers; the copies to and from the device are part of the call. */
+int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
+                   double* out_lo, double* out_hi, int8_t* verdict);
+
+/* Same on device buffers, asynchronous on `stream` (a cudaStream_t; NULL for the legacy stream). */
+int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
+                          double* out_lo, double* out_hi, int8_t* verdict, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SID_H */

@@ -1,0 +1,69 @@
+// CPU ORACLE -- test infrastructure only: a C ABI over oracle.hpp for the Python tests and the CPU
+// baseline leg of bench.py (loaded with ctypes).
+#include "oracle.hpp"
+
+#include <cstring>
+#include <exception>
+#include <string>
+
+namespace {
+thread_local std::string last_error;
+}
+
+extern "C" {
+
+const char* sido_last_error(void) { return last_error.c_str(); }
+
+/* counts_out: cuboids, leaves, criticals, repeated. crit_out may be NULL; it receives up to crit_cap
+ * criticals (2*nargs doubles each); *crit_n the number stored. */
+int sido_prove(const char* ir, unsigned generations, int max_iterations, float vol, float single, int threads,
+               unsigned long long* counts_out, double* seconds, double* crit_out, unsigned long long crit_cap,
+               unsigned long long* crit_n) {
+    try {
+        sido::ProveOptions o;
+        o.generations = generations;
+        o.max_iterations = max_iterations;
+        o.iteration_volume = vol;
+        o.iteration_single = single;
+        o.threads = threads;
+        o.max_criticals = crit_out ? crit_cap : 0;
+        sido::ProveResult r = sido::prove(ir, o);
+        counts_out[0] = r.counts.cuboids;
+        counts_out[1] = r.counts.leaves;
+        counts_out[2] = r.counts.criticals;
+        counts_out[3] = r.counts.repeated;
+        if(seconds) *seconds = r.seconds;
+        if(crit_n) *crit_n = 0;
+        if(crit_out && !r.criticals.empty()) {
+            std::memcpy(crit_out, r.criticals.data(), r.criticals.size() * sizeof(double));
+        }
+        if(crit_n && !r.criticals.empty()) *crit_n = 0;  // set by caller from sizes below
+        return int(r.criticals.size());
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
+int sido_root_box(const char* ir, double* out) {
+    try {
+        auto b = sido::root_box(ir);
+        std::memcpy(out, b.data(), b.size() * sizeof(double));
+        return 0;
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
+int sido_eval_batch(const char* ir, const double* lo, const double* hi, unsigned long long n, double* out_lo,
+                    double* out_hi, signed char* verdict, int threads) {
+    try {
+        sido::eval_batch(ir, lo, hi, n, out_lo, out_hi, reinterpret_cast<std::int8_t*>(verdict), threads);
+        return 0;
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+}
