@@ -15,7 +15,7 @@ extern "C" {
 const char* sido_last_error(void) { return last_error.c_str(); }
 
 /* counts_out: cuboids, leaves, criticals, repeated. crit_out may be NULL; it receives up to crit_cap
- * criticals (2*nargs doubles each); *crit_n the number stored. */
+ * criticals (2*nargs doubles each); *crit_n receives the number of stored (lo,hi) pairs. */
 int sido_prove(const char* ir, unsigned generations, int max_iterations, float vol, float single, int threads,
                unsigned long long* counts_out, double* seconds, double* crit_out, unsigned long long crit_cap,
                unsigned long long* crit_n) {
@@ -33,12 +33,11 @@ int sido_prove(const char* ir, unsigned generations, int max_iterations, float v
         counts_out[2] = r.counts.criticals;
         counts_out[3] = r.counts.repeated;
         if(seconds) *seconds = r.seconds;
-        if(crit_n) *crit_n = 0;
         if(crit_out && !r.criticals.empty()) {
             std::memcpy(crit_out, r.criticals.data(), r.criticals.size() * sizeof(double));
         }
-        if(crit_n && !r.criticals.empty()) *crit_n = 0;  // set by caller from sizes below
-        return int(r.criticals.size());
+        if(crit_n) *crit_n = r.criticals.empty() ? 0 : (unsigned long long)(r.criticals.size()) / 2ull;
+        return 0;
     } catch(const std::exception& e) {
         last_error = e.what();
         return -1;

@@ -1,0 +1,84 @@
+"""CPU ORACLE -- test infrastructure only: ctypes binding of oracle/_build/liboracle.so.
+
+Used by tests/ and by the CPU-baseline leg of bench.py; never by the product.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "-j4"], check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = ctypes.CDLL(LIB)
+        _lib.sido_prove.restype = ctypes.c_int
+        _lib.sido_prove.argtypes = [ctypes.c_char_p, ctypes.c_uint, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.c_void_p, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)]
+        _lib.sido_root_box.restype = ctypes.c_int
+        _lib.sido_root_box.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
+        _lib.sido_eval_batch.restype = ctypes.c_int
+        _lib.sido_eval_batch.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_ulonglong,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        _lib.sido_last_error.restype = ctypes.c_char_p
+    return _lib
+
+
+def _err():
+    return lib().sido_last_error().decode()
+
+
+def prove(ir_text, generations=8, max_iterations=1, threads=0, max_criticals=0, nargs=None):
+    """Run the oracle proof; returns dict(cuboids, leaves, criticals, repeated, seconds, boxes)."""
+    L = lib()
+    counts = (ctypes.c_ulonglong * 4)()
+    secs = ctypes.c_double()
+    n_pairs = ctypes.c_ulonglong(0)
+    buf = None
+    if max_criticals:
+        if nargs is None:
+            nargs = int([l for l in ir_text.splitlines() if l.startswith("nargs ")][0].split()[1])
+        buf = np.zeros(max_criticals * 2 * nargs, dtype=np.float64)
+    rc = L.sido_prove(ir_text.encode(), generations, max_iterations, 0.25, 0.66, threads, counts, ctypes.byref(secs),
+                      buf.ctypes.data if buf is not None else None, max_criticals, ctypes.byref(n_pairs))
+    if rc != 0:
+        raise RuntimeError("oracle: " + _err())
+    out = dict(cuboids=counts[0], leaves=counts[1], criticals=counts[2], repeated=counts[3], seconds=secs.value)
+    if buf is not None:
+        out["boxes"] = buf[: n_pairs.value * 2].reshape(-1, nargs, 2)
+    return out
+
+
+def root_box(ir_text, nargs):
+    out = np.zeros(2 * nargs, dtype=np.float64)
+    if lib().sido_root_box(ir_text.encode(), out.ctypes.data) != 0:
+        raise RuntimeError("oracle: " + _err())
+    return out.reshape(nargs, 2)
+
+
+def eval_batch(ir_text, lo, hi, threads=0):
+    """lo, hi: float64 arrays of shape (nargs, n). Returns (out_lo, out_hi, verdict)."""
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    n = lo.shape[1]
+    out_lo = np.empty_like(lo)
+    out_hi = np.empty_like(hi)
+    verdict = np.empty(n, dtype=np.int8)
+    rc = lib().sido_eval_batch(ir_text.encode(), lo.ctypes.data, hi.ctypes.data, n, out_lo.ctypes.data,
+                               out_hi.ctypes.data, verdict.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError("oracle: " + _err())
+    return out_lo, out_hi, verdict

@@ -1,0 +1,405 @@
+#!/usr/bin/env python3
+"""Generate CUDA device code for compiled lemmas.
+
+For every lemma IR file (written by the front end, include/ivarp/sid_fe/compile.hpp) this emits one
+.cu translation unit with a lemma type `L` providing, for the frontier kernels of engine.cuh:
+
+  * apply_bound<T>(k, box): evaluate bound function k on the box and apply it to its target
+    variable (straight-line interval code, common subexpressions shared, if_then_else branches
+    evaluated only when needed, like the reference's if_then_else evaluation);
+  * rows_ok<T>(r0, r1, box): do all constraints of rows [r0, r1) possibly hold (stops at the first
+    violated constraint, like CPUProverCore::p_cuboid_violates_constraint_row);
+  * the update lists as 64-bit masks, the targets and the compile-time variable bounds.
+
+Interval operations whose case analysis depends on compile-time bounds get those decisions as
+template arguments (see interval.cuh). The code is generic in the number type T so the same lemma
+can run in double (the reference's IDouble) and float.
+
+  python codegen.py --out DIR lemma1.sidir lemma2.sidir ...
+"""
+import argparse
+import os
+import re
+import sys
+
+FXMAX = 9223372036854775807
+FXMIN = -FXMAX
+FX_ONE = 1000000
+
+OPS = ["arg", "const", "bconst", "neg", "add", "sub", "mul", "div", "sqrt", "pow", "acos", "asin", "min",
+       "max", "ite", "lt", "le", "gt", "ge", "eq", "ne", "orseq", "andseq", "or", "and", "not"]
+PRED_OPS = {"bconst", "lt", "le", "gt", "ge", "eq", "ne", "orseq", "andseq", "or", "and", "not"}
+
+
+class Node:
+    __slots__ = ("id", "op", "lb", "ub", "aux", "ch")
+
+    def __init__(self, nid, op, lb, ub, aux, ch):
+        self.id, self.op, self.lb, self.ub, self.aux, self.ch = nid, op, lb, ub, aux, ch
+
+
+class Lemma:
+    def __init__(self, path):
+        self.path = path
+        self.slug = os.path.splitext(os.path.basename(path))[0]
+        self.consts, self.nodes, self.bounds, self.constraints = [], [], [], []
+        self.upd = {}
+        self.rows = {}
+        self.ct = {}
+        self.splits = []
+        text = open(path).read()
+        self.text = text
+        for line in text.splitlines():
+            t = line.split()
+            if not t:
+                continue
+            kw = t[0]
+            if kw == "numtype":
+                self.numtype = t[1]
+            elif kw == "nargs":
+                self.nargs = int(t[1])
+            elif kw == "arg":
+                self.ct[int(t[1])] = (int(t[3]), int(t[4]))
+            elif kw == "split":
+                self.splits.append(tuple(int(x) for x in t[1:]))
+            elif kw == "const":
+                self.consts.append((t[2], t[3], t[4], t[5], int(t[6])))
+            elif kw == "node":
+                nc = int(t[6])
+                self.nodes.append(Node(int(t[1]), t[2], int(t[3]), int(t[4]), int(t[5]), [int(x) for x in t[7:7 + nc]]))
+            elif kw == "bound":
+                self.bounds.append((int(t[2]), {"leq": 1, "geq": 2, "both": 3}[t[3]], int(t[4]), int(t[5])))
+            elif kw == "update":
+                self.upd[(int(t[1]), t[2])] = [int(x) for x in t[4:]]
+            elif kw == "constraint":
+                self.constraints.append(int(t[2]))
+            elif kw == "row":
+                self.rows[int(t[1])] = [int(x) for x in t[3:]]
+        self.fingerprint = fingerprint(text)
+        if len(self.bounds) > 64:
+            raise ValueError("%s: more than 64 bounds are not supported" % path)
+
+    def uses(self, op):
+        return any(n.op == op for n in self.nodes)
+
+
+def fingerprint(text):
+    """FNV-1a over the IR lines except the name line (same as lemma_ir.hpp)."""
+    h = 1469598103934665603
+    for line in text.split("\n")[:-1] if text.endswith("\n") else text.split("\n"):
+        if line.startswith("name "):
+            continue
+        for c in line.encode():
+            h ^= c
+            h = (h * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+        h ^= 10
+        h = (h * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def tri_nn(n):
+    return 1 if n.lb >= 0 else (0 if n.ub <= 0 else -1)
+
+
+def tri_np(n):
+    return 1 if n.ub <= 0 else (0 if n.lb >= 0 else -1)
+
+
+def tri_pos(n):
+    return 1 if n.lb > 0 else (0 if n.ub <= 0 else -1)
+
+
+def tri_neg(n):
+    return 1 if n.ub < 0 else (0 if n.lb >= 0 else -1)
+
+
+def finite(n):
+    return n.lb > FXMIN and n.ub < FXMAX
+
+
+def float_literal(hexstr):
+    # "%a" output of a float value printed as double; append the f suffix after an exponent
+    return hexstr + "f" if "p" in hexstr else hexstr + ".0f"
+
+
+class Emitter:
+    def __init__(self, lemma):
+        self.L = lemma
+        self.lines = []
+        self.counter = 0
+        self.indent = 1
+
+    def fresh(self, prefix):
+        self.counter += 1
+        return "%s%d" % (prefix, self.counter)
+
+    def emit(self, s):
+        self.lines.append("    " * self.indent + s)
+
+    def expr(self, nid, scope):
+        if nid in scope:
+            return scope[nid]
+        n = self.L.nodes[nid]
+        op = n.op
+        if op in PRED_OPS:
+            raise ValueError("predicate node %d used as expression" % nid)
+        if op == "arg":
+            name = "box[%d]" % n.aux
+            scope[nid] = name
+            return name
+        name = self.fresh("v")
+        if op == "const":
+            dlo, dhi, flo, fhi, und = self.L.consts[n.aux]
+            self.emit("const Iv<T> %s = cst<T>(%s, %s, %s, %s, %s);" % (
+                name, dlo, dhi, float_literal(flo), float_literal(fhi), "true" if und else "false"))
+        elif op == "ite":
+            c = self.pred(n.ch[0], scope)
+            t_name, e_name = self.fresh("t"), self.fresh("e")
+            self.emit("Iv<T> %s{T(0), T(0), false}, %s{T(0), T(0), false};" % (t_name, e_name))
+            self.emit("if(%s.ub) {" % c)
+            self.indent += 1
+            inner = dict(scope)
+            self.emit("%s = %s;" % (t_name, self.expr(n.ch[1], inner)))
+            self.indent -= 1
+            self.emit("}")
+            self.emit("if(!%s.lb) {" % c)
+            self.indent += 1
+            inner = dict(scope)
+            self.emit("%s = %s;" % (e_name, self.expr(n.ch[2], inner)))
+            self.indent -= 1
+            self.emit("}")
+            self.emit("const Iv<T> %s = %s.lb ? %s : (!%s.ub ? %s : iv_join(%s, %s));" % (
+                name, c, t_name, c, e_name, t_name, e_name))
+        else:
+            ch = [self.expr(c, scope) for c in n.ch]
+            cn = [self.L.nodes[c] for c in n.ch]
+            if op == "neg":
+                rhs = "iv_neg(%s)" % ch[0]
+            elif op == "add":
+                rhs = "iv_add(%s, %s)" % (ch[0], ch[1])
+            elif op == "sub":
+                rhs = "iv_sub(%s, %s)" % (ch[0], ch[1])
+            elif op == "mul":
+                rhs = "iv_mul<T, %d, %d, %d, %d, %s>(%s, %s)" % (
+                    tri_nn(cn[0]), tri_np(cn[0]), tri_nn(cn[1]), tri_np(cn[1]),
+                    "true" if finite(cn[0]) and finite(cn[1]) else "false", ch[0], ch[1])
+            elif op == "div":
+                rhs = "iv_div<T, %d, %d, %d, %d, %s>(%s, %s)" % (
+                    tri_nn(cn[0]), tri_np(cn[0]), tri_pos(cn[1]), tri_neg(cn[1]),
+                    "true" if finite(cn[0]) and finite(cn[1]) else "false", ch[0], ch[1])
+            elif op == "sqrt":
+                rhs = "iv_sqrt<T, %d>(%s)" % (tri_nn(cn[0]), ch[0])
+            elif op == "pow":
+                rhs = "iv_pow<T, %du>(%s)" % (n.aux, ch[0])
+            elif op in ("min", "max"):
+                acc = ch[-1]
+                for x in reversed(ch[:-1]):
+                    acc = "iv_%s(%s, %s)" % (op, x, acc)
+                rhs = acc
+            elif op == "acos":
+                rhs = "iv_acos<T, %s, %s>(%s)" % ("true" if cn[0].lb < -FX_ONE else "false",
+                                                  "true" if cn[0].ub > FX_ONE else "false", ch[0])
+            else:
+                raise ValueError("unsupported expression operation %s" % op)
+            self.emit("const Iv<T> %s = %s;" % (name, rhs))
+        scope[nid] = name
+        return name
+
+    def pred(self, nid, scope):
+        if nid in scope:
+            return scope[nid]
+        n = self.L.nodes[nid]
+        op = n.op
+        if op not in PRED_OPS:
+            raise ValueError("expression node %d used as predicate" % nid)
+        name = self.fresh("p")
+        if n.lb == n.ub:
+            v = "true" if n.lb else "false"
+            self.emit("const IB %s{%s, %s};" % (name, v, v))
+        elif op in ("lt", "le", "gt", "ge", "eq", "ne"):
+            a = self.expr(n.ch[0], scope)
+            b = self.expr(n.ch[1], scope)
+            self.emit("const IB %s = iv_%s(%s, %s);" % (name, op, a, b))
+        elif op in ("orseq", "andseq"):
+            is_or = op == "orseq"
+            self.emit("IB %s{%s, %s};" % (name, "false" if is_or else "true", "false" if is_or else "true"))
+            opened = 0
+            for i, c in enumerate(n.ch):
+                sub = scope if i == 0 else dict(scope)
+                if i > 0:
+                    self.emit("if(%s%s) {" % ("!" if is_or else "", name + (".lb" if is_or else ".ub")))
+                    self.indent += 1
+                    opened += 1
+                x = self.pred(c, sub)
+                if is_or:
+                    self.emit("%s.lb = %s.lb || %s.lb; %s.ub = %s.ub || %s.ub;" % (name, name, x, name, name, x))
+                else:
+                    self.emit("%s.lb = %s.lb && %s.lb; %s.ub = %s.ub && %s.ub;" % (name, name, x, name, name, x))
+            for _ in range(opened):
+                self.indent -= 1
+                self.emit("}")
+            if is_or:
+                self.emit("if(%s.lb) %s.ub = true;" % (name, name))
+            else:
+                self.emit("if(!%s.ub) %s.lb = false;" % (name, name))
+        elif op in ("or", "and"):
+            xs = [self.pred(c, scope) for c in n.ch]
+            j = " || " if op == "or" else " && "
+            self.emit("const IB %s{%s, %s};" % (name, j.join(x + ".lb" for x in xs), j.join(x + ".ub" for x in xs)))
+        elif op == "not":
+            x = self.pred(n.ch[0], scope)
+            self.emit("const IB %s = ib_not(%s);" % (name, x))
+        elif op == "bconst":
+            self.emit("const IB %s{%s, %s};" % (name, "true" if n.lb else "false", "true" if n.ub else "false"))
+        else:
+            raise ValueError("unsupported predicate operation %s" % op)
+        scope[nid] = name
+        return name
+
+
+def mask(ids):
+    m = 0
+    for i in ids:
+        m |= 1 << i
+    return m
+
+
+def generate(lemma):
+    L = lemma
+    T_plain = "float" if L.numtype == "f32" else "double"
+    ns = "lemma_" + re.sub(r"[^A-Za-z0-9_]", "_", L.slug)
+    out = []
+    w = out.append
+    w("// Generated by csrc/codegen.py from lemmas/%s -- do not edit." % os.path.basename(L.path))
+    w('#include "engine.cuh"')
+    w('#include "acos.cuh"')
+    w("")
+    w("namespace sid {")
+    w("namespace %s {" % ns)
+    w("")
+    w("struct L {")
+    w("    static constexpr int NARGS = %d;" % L.nargs)
+    w("    static constexpr int NBOUNDS = %d;" % len(L.bounds))
+    for kind in ("lb", "ub", "both"):
+        w("    __device__ __forceinline__ static std::uint64_t upd_%s(int a) {" % kind)
+        w("        switch(a) {")
+        for a in range(L.nargs):
+            m = mask(L.upd.get((a, kind), []))
+            if m:
+                w("            case %d: return 0x%xull;" % (a, m))
+        w("            default: return 0ull;")
+        w("        }")
+        w("    }")
+    w("    __device__ __forceinline__ static int target(int k) {")
+    w("        switch(k) {")
+    for k, b in enumerate(L.bounds):
+        w("            case %d: return %d;" % (k, b[0]))
+    w("            default: return 0;")
+    w("        }")
+    w("    }")
+    for which, idx in (("lb", 0), ("ub", 1)):
+        w("    __device__ __forceinline__ static long long ct_%s(int v) {" % which)
+        w("        switch(v) {")
+        for a in range(L.nargs):
+            w("            case %d: return %dll;" % (a, L.ct[a][idx]))
+        w("            default: return 0ll;")
+        w("        }")
+        w("    }")
+    w("    template<class T> __device__ static int apply_bound(int k, Iv<T>* box);")
+    w("    template<class T> __device__ static bool rows_ok(int r0, int r1, const Iv<T>* box);")
+    for r in range(L.nargs):
+        w("    template<class T> __device__ static bool row_%d(const Iv<T>* box);" % r)
+    w("};")
+    w("")
+    # bound functions
+    w("template<class T> __device__ int L::apply_bound(int k, Iv<T>* box) {")
+    w("    switch(k) {")
+    for k, (tgt, d, fn, defined) in enumerate(L.bounds):
+        e = Emitter(L)
+        e.indent = 2
+        v = e.expr(fn, {})
+        w("    case %d: {" % k)
+        out.extend(e.lines)
+        w("        return apply_to<%d, %s>(box[%d], %s);" % (d, "true" if defined else "false", tgt, v))
+        w("    }")
+    w("    default: return B_NONE;")
+    w("    }")
+    w("}")
+    w("")
+    for r in range(L.nargs):
+        w("template<class T> __device__ bool L::row_%d(const Iv<T>* box) {" % r)
+        e = Emitter(L)
+        scope = {}
+        for ci in L.rows.get(r, []):
+            p = e.pred(L.constraints[ci], scope)
+            e.emit("if(!%s.ub) return false;" % p)
+        out.extend(e.lines)
+        w("    return true;")
+        w("}")
+        w("")
+    w("template<class T> __device__ bool L::rows_ok(int r0, int r1, const Iv<T>* box) {")
+    w("    for(int r = r0; r < r1; ++r) {")
+    w("        bool ok = true;")
+    w("        switch(r) {")
+    for r in range(L.nargs):
+        w("            case %d: ok = row_%d<T>(box); break;" % (r, r))
+        pass
+    w("            default: break;")
+    w("        }")
+    w("        if(!ok) return false;")
+    w("    }")
+    w("    return true;")
+    w("}")
+    w("")
+    w("static cudaError_t level(int mode, const LevelArgs& a, cudaStream_t s) { return launch_level<L, %s>(mode, a, s); }" % T_plain)
+    w("static cudaError_t root_box(double2* o, cudaStream_t s) { return launch_root_box<L, %s>(o, s); }" % T_plain)
+    w("static cudaError_t eval_batch(const BatchArgs& a, cudaStream_t s) { return launch_eval_batch<L, %s>(a, s); }" % T_plain)
+    w("")
+    w("} // namespace %s" % ns)
+    w("")
+    w("extern const LemmaKernels kernels_%s;" % ns)
+    w("const LemmaKernels kernels_%s = {\"%s\", 0x%016xull, %d, %d, %s, &%s::level, &%s::root_box, &%s::eval_batch};" % (
+        ns, L.slug, L.fingerprint, L.nargs, len(L.bounds), "true" if L.numtype == "f32" else "false", ns, ns, ns))
+    w("")
+    w("} // namespace sid")
+    return ns, "\n".join(out) + "\n"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", required=True)
+    ap.add_argument("irs", nargs="+")
+    args = ap.parse_args()
+    os.makedirs(args.out, exist_ok=True)
+    names = []
+    for p in args.irs:
+        lemma = Lemma(p)
+        ns, code = generate(lemma)
+        dest = os.path.join(args.out, ns + ".cu")
+        old = open(dest).read() if os.path.exists(dest) else None
+        if old != code:
+            with open(dest, "w") as f:
+                f.write(code)
+        names.append(ns)
+    reg = ["// Generated by csrc/codegen.py -- do not edit.", '#include "engine.cuh"', "", "namespace sid {"]
+    for ns in names:
+        reg.append("extern const LemmaKernels kernels_%s;" % ns)
+    reg.append("extern const LemmaKernels* const kAllLemmas[] = {")
+    for ns in names:
+        reg.append("    &kernels_%s," % ns)
+    reg.append("};")
+    reg.append("extern const int kNumLemmas = %d;" % len(names))
+    reg.append("} // namespace sid")
+    code = "\n".join(reg) + "\n"
+    dest = os.path.join(args.out, "registry.cu")
+    old = open(dest).read() if os.path.exists(dest) else None
+    if old != code:
+        with open(dest, "w") as f:
+            f.write(code)
+    for ns in names:
+        print(os.path.join(args.out, ns + ".cu"))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,363 @@
+// Frontier kernels of the GB300 prover engine, templated on a generated lemma type L.
+//
+// The reference processes one queue element at a time on a CPU thread, recursing over the static
+// splits (cpu_prover/cpu_prover_core.hpp:221-256) and the dynamic re-splits
+// (prover/pd_impl_split_into.hpp:37-66). Here each recursion level is one data-parallel launch over
+// all (item, child) pairs of a whole batch of elements:
+//   * one thread per child: split the parent's variable (splitter.hpp:44-59), propagate bounds with
+//     the reference's worklist semantics, test the constraint rows;
+//   * survivors of inner levels are compacted into the next level's list with one atomic per warp
+//     (ballot + popc); survivors of the innermost static level are joined into their element's hull
+//     with lock-free 64-bit atomics (ordered keys), or stored as criticals in the final generation.
+// Counts are order independent (the reference sums per-thread counters), so the level-synchronous
+// traversal reproduces them exactly.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "interval.cuh"
+
+namespace sid {
+
+enum BoundResult : int { B_NONE = 0, B_LB = 1, B_UB = 2, B_BOTH = 3, B_EMPTY = 4 };
+
+/// Applies a bound function value v to the target interval (CompileTimeBound::apply_to,
+/// constraints_to_bounds/compile_time_bound.hpp:42-85).
+template<int DIR, bool DEFINED, class T> __device__ __forceinline__ int apply_to(Iv<T>& t, const Iv<T>& v) {
+    if(!DEFINED && v.und) return B_NONE;
+    if(DIR == 1) {
+        if(v.hi < t.hi) { t.hi = v.hi; return v.hi < t.lo ? B_EMPTY : B_UB; }
+        return B_NONE;
+    } else if(DIR == 2) {
+        if(v.lo > t.lo) { t.lo = v.lo; return v.lo > t.hi ? B_EMPTY : B_LB; }
+        return B_NONE;
+    } else {
+        int ch = B_NONE;
+        if(v.hi < t.hi) { t.hi = v.hi; ch |= B_UB; }
+        if(v.lo > t.lo) { t.lo = v.lo; ch |= B_LB; }
+        return (t.hi < t.lo) ? B_EMPTY : ch;
+    }
+}
+
+template<class T> __device__ __forceinline__ Iv<T> cst(double dlo, double dhi, float flo, float fhi, bool und);
+template<> __device__ __forceinline__ Iv<double> cst<double>(double dlo, double dhi, float, float, bool und) {
+    return {dlo, dhi, und};
+}
+template<> __device__ __forceinline__ Iv<float> cst<float>(double, double, float flo, float fhi, bool und) {
+    return {flo, fhi, und};
+}
+
+/// Worklist bound propagation after a change of variable `arg` (both bounds), with the reference's
+/// FIFO order, de-duplication, per-bound recursion limit and "unstable" re-seeding between
+/// iterations (bound_propagation/iterated_recursive.hpp:59-131, dynamic_bound_application.hpp:104-123,
+/// index_queue_set.hpp:38-101). Returns true if the box became empty.
+template<class L, class T> __device__ bool propagate(int arg, Iv<T>* box, int it_limit, int rec_limit) {
+    constexpr int NB = L::NBOUNDS;
+    if(NB == 0) return false;
+    const std::uint64_t seed = L::upd_both(arg);
+    if(!seed) return false;
+    std::uint8_t ring[NB > 0 ? NB : 1];
+    std::uint8_t rec[NB > 0 ? NB : 1];
+    std::uint8_t ulist[NB > 0 ? NB : 1];
+    #pragma unroll
+    for(int i = 0; i < NB; ++i) rec[i] = 0;
+    std::uint64_t present = 0, unstable = 0;
+    int qb = 0, qe = 0, qn = 0, nun = 0;
+    for(std::uint64_t m = seed; m; m &= m - 1) {
+        int a = __ffsll((long long)m) - 1;
+        present |= (1ull << a);
+        ring[qe] = std::uint8_t(a);
+        qe = (qe + 1 == NB) ? 0 : qe + 1;
+        ++qn;
+    }
+    for(int it = 0; it < it_limit; ++it) {
+        while(qn > 0) {
+            int k = ring[qb];
+            present &= ~(1ull << k);
+            qb = (qb + 1 == NB) ? 0 : qb + 1;
+            --qn;
+            int r = L::template apply_bound<T>(k, box);
+            if(r == B_EMPTY) return true;
+            if(r == B_NONE) continue;
+            const int tgt = L::target(k);
+            std::uint64_t upd = r == B_LB ? L::upd_lb(tgt) : (r == B_UB ? L::upd_ub(tgt) : L::upd_both(tgt));
+            for(; upd; upd &= upd - 1) {
+                int a = __ffsll((long long)upd) - 1;
+                std::uint64_t bit = 1ull << a;
+                if(rec[a] >= rec_limit) {
+                    if(!(present & bit) && !(unstable & bit)) {
+                        ulist[nun++] = std::uint8_t(a);
+                        unstable |= bit;
+                    }
+                } else if(!(present & bit)) {
+                    present |= bit;
+                    ring[qe] = std::uint8_t(a);
+                    qe = (qe + 1 == NB) ? 0 : qe + 1;
+                    ++qn;
+                    rec[a] += 1;
+                }
+            }
+        }
+        if(nun == 0) break;
+        for(int j = 0; j < nun; ++j) {
+            int a = ulist[j];
+            std::uint64_t bit = 1ull << a;
+            if(!(present & bit)) {
+                present |= bit;
+                ring[qe] = std::uint8_t(a);
+                qe = (qe + 1 == NB) ? 0 : qe + 1;
+                ++qn;
+            }
+        }
+        #pragma unroll
+        for(int i = 0; i < NB; ++i) rec[i] = 0;
+        unstable = 0;
+        nun = 0;
+    }
+    return false;
+}
+
+/// Splitter::subrange (splitter.hpp:44-59): width (ub-lb)/n and points lb + i*w, all rounded down
+/// like the reference's global rounding mode; the last point is exactly ub.
+template<class T> __device__ __forceinline__ void split_child(T lb, T ub, int n, int i, T& lo, T& hi) {
+    T w = Dir<T>::div_rd(Dir<T>::sub_rd(ub, lb), T(n));
+    lo = (i >= n) ? ub : Dir<T>::add_rd(lb, Dir<T>::mul_rd(T(i), w));
+    hi = (i + 1 >= n) ? ub : Dir<T>::add_rd(lb, Dir<T>::mul_rd(T(i + 1), w));
+}
+
+enum LevelMode : int {
+    MODE_EMIT = 0,       // survivors go to the next level's list (path = path*n + child)
+    MODE_HULL = 1,       // innermost static level: survivors are leaves joined into the element hull
+    MODE_CRIT = 2,       // innermost static level of the final generation: survivors are criticals
+    MODE_QUEUE = 3       // last dynamic level (root partition / re-split): survivors become queue elements
+};
+
+/// Order-preserving 64-bit keys for atomicMin/atomicMax on doubles; -0 and +0 share a key.
+__device__ __forceinline__ unsigned long long order_key(double v) {
+    long long b = __double_as_longlong(v == 0.0 ? 0.0 : v);
+    return (unsigned long long)(b < 0 ? ~b : (b | (long long)0x8000000000000000ull));
+}
+__device__ __forceinline__ double key_value(unsigned long long k) {
+    long long b = (long long)((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k);
+    return __longlong_as_double(b);
+}
+
+struct LevelArgs {
+    // input items: boxes in structure-of-arrays layout box[v*stride + i] (lo, hi)
+    const double2* in_box;
+    std::uint64_t in_stride;
+    const std::uint32_t* in_elem;     // element index of each item (nullptr: item index + elem_base)
+    const std::uint64_t* in_path;     // leaf-order path (nullptr: 0)
+    const std::uint8_t* in_depth;     // depth of each item (MODE_QUEUE; nullptr: depth_value)
+    std::uint64_t in_begin, n_in;     // items [in_begin, in_begin + n_in)
+    std::uint32_t elem_base;
+    int var, nsub, it_limit, rec_limit;
+    int row_begin, row_end;           // constraint rows to test (row_end <= row_begin: none)
+    std::uint8_t depth_value;         // depth for MODE_QUEUE when in_depth is null
+    std::uint8_t depth_add;           // added to the input depth for MODE_QUEUE
+    // outputs (MODE_EMIT / MODE_QUEUE)
+    double2* out_box;
+    std::uint64_t out_stride, out_cap;
+    std::uint32_t* out_elem;
+    std::uint64_t* out_path;
+    std::uint8_t* out_depth;
+    unsigned long long* out_count;    // slots already used on entry
+    // hull (MODE_HULL): per element and variable
+    unsigned long long* hull_lo;      // order keys, min
+    unsigned long long* hull_hi;      // order keys, max
+    unsigned long long* hull_zlo;     // (path<<1 | sign) of the first leaf whose lo is zero
+    unsigned long long* hull_zhi;
+    // criticals (MODE_CRIT): 2*nargs doubles each
+    double* crit;
+    std::uint64_t crit_cap;
+    unsigned long long* crit_count;
+    // counters
+    unsigned long long* leaf_count;
+    unsigned int* overflow;           // set when an output list would overflow
+};
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+template<class L, class T, int MODE> __global__ void __launch_bounds__(128) k_level(const LevelArgs a) {
+    constexpr int N = L::NARGS;
+    const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
+    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(t >= total) return;
+    const unsigned active = __activemask();
+    const std::uint64_t item = a.in_begin + t / std::uint64_t(a.nsub);
+    const int c = int(t % std::uint64_t(a.nsub));
+
+    Iv<T> box[N];
+    #pragma unroll
+    for(int v = 0; v < N; ++v) {
+        double2 b = a.in_box[std::uint64_t(v) * a.in_stride + item];
+        box[v] = {T(b.x), T(b.y), false};
+    }
+    {
+        T lo, hi;
+        split_child(box[a.var].lo, box[a.var].hi, a.nsub, c, lo, hi);
+        box[a.var] = {lo, hi, false};
+    }
+    bool ok = !propagate<L, T>(a.var, box, a.it_limit, a.rec_limit);
+    if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<T>(a.row_begin, a.row_end, box);
+
+    unsigned long long leaves = ok ? 0ull : 1ull;
+    if(MODE == MODE_HULL || MODE == MODE_CRIT) leaves = 1ull;
+
+    if(MODE == MODE_EMIT || MODE == MODE_QUEUE) {
+        const unsigned m = __ballot_sync(active, ok);
+        const int leader = __ffs(active) - 1;
+        unsigned long long base = 0;
+        if(int(lane_id()) == leader && m) base = atomicAdd(a.out_count, (unsigned long long)__popc(m));
+        base = __shfl_sync(active, base, leader);
+        if(ok) {
+            const std::uint64_t slot = base + __popc(m & ((1u << lane_id()) - 1u));
+            if(slot < a.out_cap) {
+                #pragma unroll
+                for(int v = 0; v < N; ++v) {
+                    a.out_box[std::uint64_t(v) * a.out_stride + slot] = make_double2(double(box[v].lo), double(box[v].hi));
+                }
+                if(MODE == MODE_EMIT && a.out_elem) {
+                    a.out_elem[slot] = a.in_elem ? a.in_elem[item] : std::uint32_t(item - a.in_begin) + a.elem_base;
+                }
+                if(MODE == MODE_EMIT && a.out_path) {
+                    std::uint64_t p = a.in_path ? a.in_path[item] : 0ull;
+                    a.out_path[slot] = p * std::uint64_t(a.nsub) + std::uint64_t(c);
+                }
+                if(a.out_depth) {
+                    std::uint8_t d = a.in_depth ? a.in_depth[item] : a.depth_value;
+                    a.out_depth[slot] = std::uint8_t(d + (MODE == MODE_QUEUE ? a.depth_add : 0));
+                }
+            } else {
+                atomicOr(a.overflow, 1u);
+            }
+        }
+    } else if(MODE == MODE_HULL) {
+        if(ok) {
+            const std::uint32_t e = a.in_elem ? a.in_elem[item] : std::uint32_t(item - a.in_begin) + a.elem_base;
+            const std::uint64_t path = (a.in_path ? a.in_path[item] : 0ull) * std::uint64_t(a.nsub) + std::uint64_t(c);
+            #pragma unroll
+            for(int v = 0; v < N; ++v) {
+                const double lo = double(box[v].lo), hi = double(box[v].hi);
+                const std::uint64_t idx = std::uint64_t(e) * N + v;
+                atomicMin(&a.hull_lo[idx], order_key(lo));
+                atomicMax(&a.hull_hi[idx], order_key(hi));
+                if(lo == 0.0) atomicMin(&a.hull_zlo[idx], (path << 1) | (__double_as_longlong(lo) < 0 ? 1ull : 0ull));
+                if(hi == 0.0) atomicMin(&a.hull_zhi[idx], (path << 1) | (__double_as_longlong(hi) < 0 ? 1ull : 0ull));
+            }
+        }
+    } else if(MODE == MODE_CRIT) {
+        if(ok) {
+            const unsigned long long slot = atomicAdd(a.crit_count, 1ull);
+            if(slot < a.crit_cap) {
+                #pragma unroll
+                for(int v = 0; v < N; ++v) {
+                    a.crit[(slot * N + v) * 2] = double(box[v].lo);
+                    a.crit[(slot * N + v) * 2 + 1] = double(box[v].hi);
+                }
+            }
+        }
+    }
+
+    // warp-aggregated leaf count (each thread contributes at most one leaf)
+    const unsigned wsum = __reduce_add_sync(active, unsigned(leaves));
+    if(int(lane_id()) == __ffs(active) - 1 && wsum) atomicAdd(a.leaf_count, (unsigned long long)wsum);
+}
+
+/// Initial runtime box: compile-time bounds (fixed point / 1e6, rounded outward) tightened by 50*nargs
+/// rounds of all bounds in table order (refactor_constraints_impl.hpp:71-101).
+template<class L, class T> __global__ void k_root_box(double2* out) {
+    if(blockIdx.x != 0 || threadIdx.x != 0) return;
+    constexpr int N = L::NARGS;
+    Iv<T> box[N];
+    for(int v = 0; v < N; ++v) {
+        long long lb = L::ct_lb(v), ub = L::ct_ub(v);
+        double dl = lb <= -0x7fffffffffffffffll ? -Dir<double>::inf() : __ddiv_rd(double(lb), 1000000.0);
+        double du = ub >= 0x7fffffffffffffffll ? Dir<double>::inf() : __ddiv_ru(double(ub), 1000000.0);
+        box[v] = {T(0), T(0), false};
+        if(sizeof(T) == sizeof(double)) {
+            box[v].lo = T(dl);
+            box[v].hi = T(du);
+        } else {
+            box[v].lo = T(__double2float_rd(dl));
+            box[v].hi = T(__double2float_ru(du));
+        }
+    }
+    for(int round = 0; round < 50 * N; ++round) {
+        for(int k = 0; k < L::NBOUNDS; ++k) {
+            if(L::template apply_bound<T>(k, box) == B_EMPTY) break;
+        }
+    }
+    for(int v = 0; v < N; ++v) out[v] = make_double2(double(box[v].lo), double(box[v].hi));
+}
+
+struct BatchArgs {
+    const double* lo; const double* hi;
+    double* out_lo; double* out_hi;
+    std::int8_t* verdict;
+    std::uint64_t n;
+};
+
+/// Leaf evaluation of independent cuboids: propagate after a change of the last variable
+/// (it_limit = nargs, rec_limit = 4) and test all constraints.
+template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(const BatchArgs a) {
+    constexpr int N = L::NARGS;
+    const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(i >= a.n) return;
+    Iv<T> box[N];
+    #pragma unroll
+    for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * a.n + i]), T(a.hi[std::uint64_t(v) * a.n + i]), false};
+    std::int8_t vd = 0;
+    if(propagate<L, T>(N - 1, box, N, 4)) vd = 1;
+    else if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
+    a.verdict[i] = vd;
+    #pragma unroll
+    for(int v = 0; v < N; ++v) {
+        a.out_lo[std::uint64_t(v) * a.n + i] = double(box[v].lo);
+        a.out_hi[std::uint64_t(v) * a.n + i] = double(box[v].hi);
+    }
+}
+
+/// Host-side launch table of one compiled lemma.
+struct LemmaKernels {
+    const char* slug;
+    std::uint64_t fingerprint;
+    int nargs;
+    int nbounds;
+    bool is_f32;
+    cudaError_t (*level)(int mode, const LevelArgs& a, cudaStream_t s);
+    cudaError_t (*root_box)(double2* out, cudaStream_t s);
+    cudaError_t (*eval_batch)(const BatchArgs& a, cudaStream_t s);
+};
+
+template<class L, class T> cudaError_t launch_level(int mode, const LevelArgs& a, cudaStream_t s) {
+    const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
+    if(total == 0) return cudaSuccess;
+    const unsigned threads = 128;
+    const std::uint64_t blocks = (total + threads - 1) / threads;
+    if(blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    switch(mode) {
+        case MODE_EMIT: k_level<L, T, MODE_EMIT><<<unsigned(blocks), threads, 0, s>>>(a); break;
+        case MODE_HULL: k_level<L, T, MODE_HULL><<<unsigned(blocks), threads, 0, s>>>(a); break;
+        case MODE_CRIT: k_level<L, T, MODE_CRIT><<<unsigned(blocks), threads, 0, s>>>(a); break;
+        case MODE_QUEUE: k_level<L, T, MODE_QUEUE><<<unsigned(blocks), threads, 0, s>>>(a); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template<class L, class T> cudaError_t launch_root_box(double2* out, cudaStream_t s) {
+    k_root_box<L, T><<<1, 1, 0, s>>>(out);
+    return cudaGetLastError();
+}
+
+template<class L, class T> cudaError_t launch_eval_batch(const BatchArgs& a, cudaStream_t s) {
+    if(a.n == 0) return cudaSuccess;
+    const unsigned threads = 128;
+    const std::uint64_t blocks = (a.n + threads - 1) / threads;
+    k_eval_batch<L, T><<<unsigned(blocks), threads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace sid

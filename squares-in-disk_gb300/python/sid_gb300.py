@@ -1,0 +1,197 @@
+"""Python binding of the GB300 prover engine (libsid.so, C ABI in include/sid.h).
+
+Used by the tests and bench.py. The library is built in-tree by squares-in-disk_gb300/build.py; this
+module never falls back to anything else: if the library or a GPU is missing, calls fail loudly.
+"""
+import ctypes
+import glob
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REPO = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "_build", "libsid.so")
+LEMMA_DIR = os.path.join(PKG, "lemmas")
+KAT_DIR = os.path.join(REPO, "tests", "golden", "kat")
+
+SID_OK = 0
+STATUS = {0: "ok", -1: "invalid", -2: "cuda", -3: "not_compiled", -4: "nomem", -5: "timeout", -6: "unsupported",
+          -7: "capacity"}
+
+EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "sid_engine_destroy",
+            "sid_lemma_register", "sid_lemma_info", "sid_lemma_root_box", "sid_prove", "sid_fetch_criticals",
+            "sid_eval_batch", "sid_eval_batch_device"]
+
+
+class SidResult(ctypes.Structure):
+    _fields_ = [("num_cuboids", ctypes.c_uint64), ("num_leaf_cuboids", ctypes.c_uint64),
+                ("num_critical_cuboids", ctypes.c_uint64), ("num_repeated_nodes", ctypes.c_uint64),
+                ("criticals_stored", ctypes.c_uint64), ("escalated", ctypes.c_uint64), ("seconds", ctypes.c_double)]
+
+
+PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p)
+
+
+class SidProveOpts(ctypes.Structure):
+    _fields_ = [("generation_count", ctypes.c_uint32), ("max_iterations_per_node", ctypes.c_int32),
+                ("iteration_volume_criterion", ctypes.c_float),
+                ("iteration_single_dimension_criterion", ctypes.c_float),
+                ("batch_elements", ctypes.c_int64), ("precision", ctypes.c_int32),
+                ("max_criticals_kept", ctypes.c_uint64), ("progress", ctypes.c_void_p),
+                ("progress_user", ctypes.c_void_p), ("progress_first_ms", ctypes.c_uint32),
+                ("progress_every_ms", ctypes.c_uint32)]
+
+
+class SidError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%s)" % (msg, STATUS.get(status, status)))
+        self.status = status
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError("engine library not built: %s (run __graft_entry__.build())" % path)
+    L = ctypes.CDLL(path)
+    L.sid_last_error.restype = ctypes.c_char_p
+    L.sid_prove_opts_default.argtypes = [ctypes.POINTER(SidProveOpts)]
+    L.sid_engine_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    L.sid_engine_destroy.argtypes = [ctypes.c_void_p]
+    L.sid_lemma_register.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int)]
+    L.sid_lemma_info.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                 ctypes.POINTER(ctypes.c_uint64)]
+    L.sid_lemma_root_box.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    L.sid_prove.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(SidProveOpts), ctypes.POINTER(SidResult)]
+    L.sid_fetch_criticals.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                                      ctypes.POINTER(ctypes.c_uint64)]
+    L.sid_eval_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.sid_eval_batch_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != SID_OK:
+        raise SidError(status, load().sid_last_error().decode())
+
+
+def lemma_ir(name):
+    """IR text of a lemma by slug (squares-in-disk_gb300/lemmas) or known-answer system (tests/golden/kat)."""
+    for d in (LEMMA_DIR, KAT_DIR):
+        p = os.path.join(d, name + ".sidir")
+        if os.path.exists(p):
+            with open(p) as f:
+                return f.read()
+    raise FileNotFoundError(name)
+
+
+def lemma_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(LEMMA_DIR, "*.sidir")))
+
+
+def ir_nargs(ir_text):
+    for line in ir_text.splitlines():
+        if line.startswith("nargs "):
+            return int(line.split()[1])
+    raise ValueError("no nargs line")
+
+
+def ir_uses(ir_text, op):
+    return any(l.startswith("node ") and l.split()[2] == op for l in ir_text.splitlines())
+
+
+class Engine:
+    def __init__(self, device=0):
+        self.L = load()
+        h = ctypes.c_void_p()
+        _check(self.L.sid_engine_create(device, ctypes.byref(h)))
+        self.h = h
+        self._ids = {}
+
+    def close(self):
+        if self.h:
+            self.L.sid_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def register(self, ir_text):
+        if ir_text in self._ids:
+            return self._ids[ir_text]
+        lid = ctypes.c_int(-1)
+        data = ir_text.encode()
+        _check(self.L.sid_lemma_register(self.h, data, len(data), ctypes.byref(lid)))
+        self._ids[ir_text] = lid.value
+        return lid.value
+
+    def root_box(self, lemma_id, nargs):
+        out = np.zeros(2 * nargs, dtype=np.float64)
+        _check(self.L.sid_lemma_root_box(self.h, lemma_id, out.ctypes.data))
+        return out.reshape(nargs, 2)
+
+    def prove(self, lemma_id, generations=8, max_iterations=1, max_criticals=1 << 20, batch=0, precision=0,
+              nargs=None, fetch=False):
+        opts = SidProveOpts()
+        self.L.sid_prove_opts_default(ctypes.byref(opts))
+        opts.generation_count = generations
+        opts.max_iterations_per_node = max_iterations
+        opts.max_criticals_kept = max_criticals
+        opts.batch_elements = batch
+        opts.precision = precision
+        res = SidResult()
+        _check(self.L.sid_prove(self.h, lemma_id, ctypes.byref(opts), ctypes.byref(res)))
+        out = dict(cuboids=res.num_cuboids, leaves=res.num_leaf_cuboids, criticals=res.num_critical_cuboids,
+                   repeated=res.num_repeated_nodes, stored=res.criticals_stored, escalated=res.escalated,
+                   seconds=res.seconds)
+        if fetch and res.criticals_stored:
+            buf = np.zeros(res.criticals_stored * 2 * nargs, dtype=np.float64)
+            got = ctypes.c_uint64()
+            _check(self.L.sid_fetch_criticals(self.h, lemma_id, buf.ctypes.data, res.criticals_stored,
+                                              ctypes.byref(got)))
+            out["boxes"] = buf[: got.value * 2 * nargs].reshape(-1, nargs, 2)
+        return out
+
+    def eval_batch(self, lemma_id, lo, hi):
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        hi = np.ascontiguousarray(hi, dtype=np.float64)
+        n = lo.shape[1]
+        out_lo = np.empty_like(lo)
+        out_hi = np.empty_like(hi)
+        verdict = np.empty(n, dtype=np.int8)
+        _check(self.L.sid_eval_batch(self.h, lemma_id, lo.ctypes.data, hi.ctypes.data, n, out_lo.ctypes.data,
+                                     out_hi.ctypes.data, verdict.ctypes.data))
+        return out_lo, out_hi, verdict
+
+    def eval_batch_device(self, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr, verdict_ptr, stream=0):
+        _check(self.L.sid_eval_batch_device(self.h, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr,
+                                            verdict_ptr, stream))
+
+
+def synthetic_batch(root, n, seed=0x5EED0001):
+    """Seeded synthetic cuboids inside a root box: per coordinate, lo uniform over the root range and the width
+    log-uniform in [2^-24, 2^-4] of the range, clipped to the box. Returns (lo, hi) of shape (nargs, n)."""
+    rng = np.random.default_rng(seed)
+    nargs = root.shape[0]
+    lo = np.empty((nargs, n), dtype=np.float64)
+    hi = np.empty((nargs, n), dtype=np.float64)
+    for v in range(nargs):
+        a, b = float(root[v, 0]), float(root[v, 1])
+        r = b - a
+        l = rng.uniform(a, b, n)
+        w = np.exp2(rng.uniform(-24.0, -4.0, n)) * r
+        lo[v] = l
+        hi[v] = np.minimum(l + w, b)
+    return lo, hi

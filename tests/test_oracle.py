@@ -1,0 +1,59 @@
+"""CPU tests of the oracle against the reference's golden numbers (published counts, known-answer tests)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import kat_expect
+import sid_gb300 as sid
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PUBLISHED = json.load(open(os.path.join(REPO, "tests", "golden", "published_counts.json")))
+
+# lemmas the oracle proves in seconds here; the four-subcontainer lemma takes ~20 s on 8 threads
+FAST = ["top_packing_1", "top_packing_2", "one_subcontainer", "two_subcontainer", "three_subcontainer",
+        "five_subcontainer", "six_subcontainer", "seven_subcontainer"]
+
+
+@pytest.mark.parametrize("name", FAST)
+def test_oracle_matches_published_counts(oracle, name):
+    r = oracle.prove(sid.lemma_ir(name))
+    assert [r["cuboids"], r["leaves"]] == PUBLISHED[name]
+    assert r["criticals"] == 0 and r["repeated"] == 0
+
+
+@pytest.mark.parametrize("variant", ["f64", "f32"])
+def test_oracle_expected_criticals(oracle, variant):
+    r = oracle.prove(sid.lemma_ir("expected_critical_" + variant), generations=2, max_criticals=1000)
+    assert {k: r[k] for k in kat_expect.EC_COUNTS} == kat_expect.EC_COUNTS
+    got = kat_expect.sort_boxes(r["boxes"])
+    want = kat_expect.sort_boxes(kat_expect.expected_critical_boxes())
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("gen", [0, 1, 2])
+@pytest.mark.parametrize("variant", ["f64", "f32"])
+def test_oracle_expected_criticals2(oracle, gen, variant):
+    r = oracle.prove(sid.lemma_ir("expected_critical2_" + variant), generations=gen,
+                     max_criticals=300000 if gen == 2 else 0)
+    assert {k: r[k] for k in kat_expect.EC2_COUNTS[gen]} == kat_expect.EC2_COUNTS[gen]
+    if gen == 2:
+        got = kat_expect.sort_boxes(r["boxes"])
+        assert np.array_equal(got, kat_expect.expected_critical2_gen2_boxes())
+
+
+@pytest.mark.parametrize("name,gens,proves", [("pos_neg1_unsat", 7, True), ("pos_neg1_sat", 7, False),
+                                              ("run_prover_unsat_f64", 11, True), ("run_prover_sat_f64", 11, False),
+                                              ("run_prover_unsat_f32", 11, True), ("run_prover_sat_f32", 11, False)])
+def test_oracle_verdicts(oracle, name, gens, proves):
+    r = oracle.prove(sid.lemma_ir(name), generations=gens)
+    assert (r["criticals"] == 0) == proves
+    assert r["cuboids"] > r["leaves"] > 0
+
+
+def test_oracle_root_box_inside_ct_bounds(oracle):
+    ir = sid.lemma_ir("one_subcontainer")
+    box = oracle.root_box(ir, 3)
+    assert box[0, 0] == 0.295 or abs(box[0, 0] - 0.295) < 1e-15
+    assert np.all(box[:, 0] <= box[:, 1])
