@@ -25,6 +25,7 @@
 
 #include "../../include/sid.h"
 #include "engine.cuh"
+#include "engine_internal.hpp"
 #include "lemma_ir.hpp"
 
 namespace sid {
@@ -34,7 +35,12 @@ extern const int kNumLemmas;
 
 namespace {
 
-thread_local std::string g_last_error;
+// fixed-size storage: reporting an error never allocates
+thread_local char g_last_error[512];
+
+void set_last_error(const char* msg) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s", msg ? msg : "");
+}
 
 struct SidError {
     int status;
@@ -62,10 +68,10 @@ template<class F> int guarded(F&& f) {
         f();
         return SID_OK;
     } catch(const SidError& e) {
-        g_last_error = e.msg;
+        set_last_error(e.msg.c_str());
         return e.status;
     } catch(const std::exception& e) {
-        g_last_error = e.what();
+        set_last_error(e.what());
         return SID_ERR_INVALID;
     }
 }
@@ -555,6 +561,29 @@ void set_device(sid_engine* e) { cuda_check(cudaSetDevice(e->device), "cudaSetDe
 
 } // namespace
 
+namespace sid {
+
+void internal_set_error(const char* msg) { set_last_error(msg); }
+
+int internal_lemma_view(sid_engine* engine, int lemma_id, LemmaView* out) {
+    if(!engine || !out || lemma_id < 0 || lemma_id >= int(engine->lemmas.size())) return SID_ERR_INVALID;
+    const Lemma* l = engine->lemmas[std::size_t(lemma_id)].get();
+    out->kernels = l->k;
+    out->device = engine->device;
+    out->nargs = l->ir.nargs;
+    out->last_static_arg = -1;
+    out->last_static_subdivisions = 0;
+    for(const auto& s : l->ir.splits) {
+        if(!s.dynamic) {
+            out->last_static_arg = s.arg;
+            out->last_static_subdivisions = int(s.subdivisions);
+        }
+    }
+    return SID_OK;
+}
+
+} // namespace sid
+
 extern "C" {
 
 void sid_prove_opts_default(sid_prove_opts* o) {
@@ -571,7 +600,7 @@ void sid_prove_opts_default(sid_prove_opts* o) {
     o->progress_every_ms = 2000;
 }
 
-const char* sid_last_error(void) { return g_last_error.c_str(); }
+const char* sid_last_error(void) { return g_last_error; }
 
 int sid_engine_create(int device, sid_engine** out) {
     return guarded([&] {
