@@ -118,6 +118,29 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
 int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
                           double* out_lo, double* out_hi, int8_t* verdict, void* stream);
 
+/* Allocation-free leaf hulls. No counterpart in the reference: it is an addition of this library.
+ *
+ * For callers that may not allocate GPU memory: a serving loop that runs under a fixed device-memory
+ * budget and must not call the allocator (which can block, fragment memory or synchronize the device)
+ * on every request, or a host application that owns all device memory through its own pool and does
+ * not let third-party code call cudaMalloc. This call allocates nothing: no cudaMalloc or cudaFree and
+ * no other allocating routine, on the host or on the device.
+ *
+ * For each of the n parent cuboids in `boxes`, split the lemma's last static variable into its
+ * configured number of pieces, propagate bounds and test the constraints (the innermost step of the
+ * prover core), and join the surviving pieces into that parent's hull. Layout of `boxes` and `hulls`
+ * (device memory): (lo, hi) pairs, variable-major: pair [v*n + i]. nonempty[i] (device) is 1 if any
+ * piece of parent i survived, else 0 and hulls for i are left untouched; *leaves (device, may be NULL)
+ * receives the number of leaves (every piece is a leaf). Asynchronous on `stream` (a cudaStream_t).
+ *
+ * Its working memory is one 8 MiB array per device inside libsid.so, held from library load until the
+ * process exits; n * nargs must be at most 262,136 (larger calls fail with SID_ERR_CAPACITY). The first
+ * call on a device looks up that array's device address; make this first call before any stream
+ * capture. All calls on a device share the array: calls whose work overlaps on the GPU (different
+ * streams or host threads) race and corrupt each other's results, so serialize them. */
+int sid_leaf_hull_noalloc(sid_engine* engine, int lemma_id, const double* boxes, uint64_t n, double* hulls,
+                          uint8_t* nonempty, unsigned long long* leaves, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

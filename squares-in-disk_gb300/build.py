@@ -77,7 +77,8 @@ def build(ir_files=None, extra_ir_dirs=(), verbose=False, jobs=None):
     for stale in set(gen_units) - wanted:
         os.remove(stale)
     gen_units = sorted(wanted)
-    units = gen_units + [os.path.join(GEN, "registry.cu"), os.path.join(CSRC, "engine.cu")]
+    units = gen_units + [os.path.join(GEN, "registry.cu"), os.path.join(CSRC, "engine.cu"),
+                         os.path.join(CSRC, "noalloc.cu")]
     headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.hpp")) +
                      [os.path.join(REPO, "include", "sid.h")])
 

@@ -21,7 +21,7 @@ STATUS = {0: "ok", -1: "invalid", -2: "cuda", -3: "not_compiled", -4: "nomem", -
 
 EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "sid_engine_destroy",
             "sid_lemma_register", "sid_lemma_info", "sid_lemma_root_box", "sid_prove", "sid_fetch_criticals",
-            "sid_eval_batch", "sid_eval_batch_device"]
+            "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc"]
 
 
 class SidResult(ctypes.Structure):
@@ -75,6 +75,8 @@ def load(path=LIB_PATH):
     L.sid_eval_batch_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p]
+    L.sid_leaf_hull_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     _lib = L
     return L
 
@@ -178,6 +180,12 @@ class Engine:
     def eval_batch_device(self, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr, verdict_ptr, stream=0):
         _check(self.L.sid_eval_batch_device(self.h, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr,
                                             verdict_ptr, stream))
+
+
+    def leaf_hull_noalloc(self, lemma_id, boxes_ptr, n, hulls_ptr, nonempty_ptr, leaves_ptr, stream=0):
+        """Allocation-free leaf hulls on caller device buffers (see sid_leaf_hull_noalloc in sid.h)."""
+        _check(self.L.sid_leaf_hull_noalloc(self.h, lemma_id, boxes_ptr, n, hulls_ptr, nonempty_ptr, leaves_ptr,
+                                            stream))
 
 
 def synthetic_batch(root, n, seed=0x5EED0001):
