@@ -1,6 +1,7 @@
 // CPU ORACLE -- test infrastructure only: a C ABI over oracle.hpp for the Python tests and the CPU
 // baseline leg of bench.py (loaded with ctypes).
 #include "oracle.hpp"
+#include "acos_cr.hpp"
 
 #include <cstring>
 #include <exception>
@@ -65,4 +66,26 @@ int sido_eval_batch(const char* ir, const double* lo, const double* hi, unsigned
         return -1;
     }
 }
+
+/* acos(x) rounded down (up == 0) or up, for double (n doubles) and float (n floats); 0 or -1. */
+int sido_acos_rounded(const double* x, unsigned long long n, int up, double* out) {
+    try {
+        for(unsigned long long i = 0; i < n; ++i) out[i] = sido::acos_rounded<double>(x[i], up != 0);
+        return 0;
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
+int sido_acos_rounded_f32(const float* x, unsigned long long n, int up, float* out) {
+    try {
+        for(unsigned long long i = 0; i < n; ++i) out[i] = sido::acos_rounded<float>(x[i], up != 0);
+        return 0;
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
 }

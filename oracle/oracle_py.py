@@ -34,6 +34,8 @@ def lib():
         _lib.sido_eval_batch.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_ulonglong,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         _lib.sido_last_error.restype = ctypes.c_char_p
+        _lib.sido_acos_rounded.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
+        _lib.sido_acos_rounded_f32.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
     return _lib
 
 
@@ -82,3 +84,13 @@ def eval_batch(ir_text, lo, hi, threads=0):
     if rc != 0:
         raise RuntimeError("oracle: " + _err())
     return out_lo, out_hi, verdict
+
+
+def acos_rounded(x, up, dtype=np.float64):
+    """acos of every element of x rounded down (up=False) or up (up=True) to dtype (float64 or float32)."""
+    x = np.ascontiguousarray(x, dtype=dtype)
+    out = np.empty_like(x)
+    fn = lib().sido_acos_rounded if dtype == np.float64 else lib().sido_acos_rounded_f32
+    if fn(x.ctypes.data, x.size, 1 if up else 0, out.ctypes.data) != 0:
+        raise RuntimeError(_err())
+    return out

@@ -62,14 +62,7 @@ def build(ir_files=None, extra_ir_dirs=(), verbose=False, jobs=None):
     sys.path.insert(0, CSRC)
     import codegen  # noqa: E402
 
-    usable = []
-    for p in ir_files:
-        lemma = codegen.Lemma(p)
-        if lemma.uses("acos") and not codegen_supports_acos():
-            if verbose:
-                print("skipping (acos not built yet):", p)
-            continue
-        usable.append(p)
+    usable = list(ir_files)
     subprocess.run([sys.executable, os.path.join(CSRC, "codegen.py"), "--out", GEN, *usable], check=True,
                    stdout=subprocess.DEVNULL if not verbose else None)
     gen_units = sorted(glob.glob(os.path.join(GEN, "lemma_*.cu")))
@@ -115,10 +108,6 @@ def build(ir_files=None, extra_ir_dirs=(), verbose=False, jobs=None):
 def _ns(path):
     import re
     return re.sub(r"[^A-Za-z0-9_]", "_", os.path.splitext(os.path.basename(path))[0])
-
-
-def codegen_supports_acos():
-    return os.path.exists(os.path.join(CSRC, "acos_impl.cuh"))
 
 
 def main():

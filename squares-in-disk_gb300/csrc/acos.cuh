@@ -1,9 +1,388 @@
-// Directed arc cosine for intervals (declaration; the lemmas that use acos are built once the
-// correctly rounded implementation is in place).
+// Correctly rounded arc cosine in a given direction, and the interval arc cosine built on it.
+//
+// The reference evaluates the interval arc cosine on the CPU with MPFR at the precision of the
+// number type: [acos(x.ub) rounded down, acos(x.lb) rounded up], after clamping the argument to
+// [-1, 1] when the compile-time bounds of the argument do not already guarantee the domain
+// (ivarp/src/interval_acos.cpp:29-34,52-66, ivarp/include/ivarp/math_fn/interval_acos.hpp:19-28,
+// interval_asin.hpp:14-32). The published cuboid counts of the lemmas that use acos depend on
+// these endpoints, so they are reproduced exactly here, on the device, without MPFR.
+//
+// Method (this file's own design; runs on the integer pipe, which is far wider than the FP64
+// pipe): acos(x) is evaluated in unsigned fixed point with NL 64-bit limbs and 64*NL-3
+// fractional bits ("units" below are 2^-(64*NL-3)),
+//   |x| <= 1/2 :  acos(x) = pi/2 - asin(x),
+//   x > 1/2    :  acos(x) = 2 asin(sqrt((1-x)/2)),
+//   x < -1/2   :  acos(x) = pi - 2 asin(sqrt((1+x)/2)),
+// with asin(t) = t * sum C_k t^(2k) (t <= 1/2, Horner, exact rational coefficients rounded to the
+// format) and sqrt(w) = w * y where y = 1/sqrt(w) is refined by Newton steps
+// y <- y (3 - w y^2) / 2 from a double start value (the argument is first scaled by an even power
+// of two into [1/4, 1)). (1-x)/2 and (1+x)/2 are exact in double.
+//
+// Error bound (all products truncated, each costs at most one unit): the series value is within
+// 4.1 + 1.4 e_t units of the exact sum for an argument with error e_t, asin within 3.1 + 1.8 e_t,
+// the square root within 3.5 units, so the result is within 19 units of acos(x); kErrUnits = 64
+// is used. The result is rounded to the target precision from the enclosure
+// [R - 64 units, R + 64 units]: when both ends round down to the same floating-point number d,
+// acos(x) lies strictly between d and its successor (acos(x) is transcendental for every
+// floating-point x except 1, Lindemann-Weierstrass), so d is the downward and its successor the
+// upward rounding. Two limbs (125 fractional bits) decide all but a vanishing fraction of the
+// arguments; the rest are evaluated again with four limbs (253 fractional bits), which is more
+// precision than any double argument needs. If even that left the rounding undecided, the result
+// would be the outward enclosure itself (still a valid bound).
+//
+// The same source compiles for the host (tests/acos_check.cpp checks it against 300-bit mpmath).
 #pragma once
 
+#include <cstdint>
+#include <cstring>
+
+#include "acos_table.cuh"
+
+#if defined(__CUDACC__)
 #include "interval.cuh"
+#endif
+
+#if defined(__CUDACC__)
+#define SID_ACOS_HD __host__ __device__
+#define SID_ACOS_NOINLINE __noinline__
+#define SID_ACOS_UNROLL _Pragma("unroll")
+#else
+#define SID_ACOS_HD
+#define SID_ACOS_NOINLINE __attribute__((noinline))
+#define SID_ACOS_UNROLL
+#endif
 
 namespace sid {
-template<class T, bool CLAMP_LO, bool CLAMP_HI> __device__ Iv<T> iv_acos(Iv<T> x);
+namespace acos_cr {
+
+#if defined(__CUDACC__)
+__constant__ const std::uint64_t kTableDev[SID_ACOS_TABLE_ROWS][4] = SID_ACOS_TABLE_INIT;
+#endif
+static const std::uint64_t kTableHost[SID_ACOS_TABLE_ROWS][4] = SID_ACOS_TABLE_INIT;
+
+constexpr int kRowPiHalf = SID_ACOS_TABLE_TERMS;
+constexpr int kRowPi = SID_ACOS_TABLE_TERMS + 1;
+constexpr std::uint64_t kErrUnits = 64;
+
+SID_ACOS_HD inline const std::uint64_t* table_row(int k) {
+#if defined(__CUDA_ARCH__)
+    return kTableDev[k];
+#else
+    return kTableHost[k];
+#endif
 }
+
+SID_ACOS_HD inline std::uint64_t bits_of(double x) {
+#if defined(__CUDA_ARCH__)
+    return static_cast<std::uint64_t>(__double_as_longlong(x));
+#else
+    std::uint64_t b;
+    std::memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+
+SID_ACOS_HD inline double double_of(std::uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double(static_cast<long long>(b));
+#else
+    double x;
+    std::memcpy(&x, &b, sizeof x);
+    return x;
+#endif
+}
+
+SID_ACOS_HD inline float float_of(std::uint32_t b) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(b);
+#else
+    float x;
+    std::memcpy(&x, &b, sizeof x);
+    return x;
+#endif
+}
+
+SID_ACOS_HD inline std::uint64_t mul_hi(std::uint64_t a, std::uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return static_cast<std::uint64_t>((static_cast<unsigned __int128>(a) * b) >> 64);
+#endif
+}
+
+SID_ACOS_HD inline int clz64(std::uint64_t v) {
+#if defined(__CUDA_ARCH__)
+    return __clzll(static_cast<long long>(v));
+#else
+    return __builtin_clzll(v);
+#endif
+}
+
+// 1/sqrt(m) for m in [1/4, 1), correctly rounded operations (any start value within 2^-40 works).
+SID_ACOS_HD inline double rsqrt_start(double m) {
+#if defined(__CUDA_ARCH__)
+    return __drcp_rn(__dsqrt_rn(m));
+#else
+    return 1.0 / __builtin_sqrt(m);
+#endif
+}
+
+// Unsigned fixed point: value = (sum w[i] 2^(64 i)) * 2^-(64 NL - 3), so values lie in [0, 8).
+template<int NL> struct Fx {
+    std::uint64_t w[NL];
+};
+
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_zero() {
+    Fx<NL> r;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) r.w[i] = 0;
+    return r;
+}
+
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_row(int k) {
+    const std::uint64_t* p = table_row(k);
+    Fx<NL> r;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) r.w[i] = p[4 - NL + i];
+    return r;
+}
+
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_units(std::uint64_t u) {
+    Fx<NL> r = fx_zero<NL>();
+    r.w[0] = u;
+    return r;
+}
+
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_int(std::uint64_t k) {   // k in [0, 8)
+    Fx<NL> r = fx_zero<NL>();
+    r.w[NL - 1] = k << 61;
+    return r;
+}
+
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_add(const Fx<NL>& a, const Fx<NL>& b) {
+    Fx<NL> r;
+    std::uint64_t c = 0;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) {
+        std::uint64_t s = a.w[i] + b.w[i];
+        std::uint64_t c1 = s < a.w[i];
+        r.w[i] = s + c;
+        c = c1 | (r.w[i] < s);
+    }
+    return r;
+}
+
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_sub(const Fx<NL>& a, const Fx<NL>& b) {   // requires a >= b
+    Fx<NL> r;
+    std::uint64_t br = 0;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) {
+        std::uint64_t d = a.w[i] - b.w[i];
+        std::uint64_t b1 = a.w[i] < b.w[i];
+        r.w[i] = d - br;
+        br = b1 | (d < br);
+    }
+    return r;
+}
+
+template<int NL> SID_ACOS_HD inline bool fx_less(const Fx<NL>& a, const Fx<NL>& b) {
+    bool less = false, decided = false;
+SID_ACOS_UNROLL
+    for(int i = NL - 1; i >= 0; --i) {
+        if(!decided && a.w[i] != b.w[i]) {
+            less = a.w[i] < b.w[i];
+            decided = true;
+        }
+    }
+    return less;
+}
+
+// Product truncated to the format (the exact 2NL-limb product shifted right by 64 NL - 3 bits);
+// both factors' product must stay below 8.
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_mul(const Fx<NL>& a, const Fx<NL>& b) {
+    std::uint64_t p[2 * NL];
+SID_ACOS_UNROLL
+    for(int i = 0; i < 2 * NL; ++i) p[i] = 0;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) {
+        std::uint64_t carry = 0;
+SID_ACOS_UNROLL
+        for(int j = 0; j < NL; ++j) {
+            std::uint64_t lo = a.w[i] * b.w[j];
+            std::uint64_t hi = mul_hi(a.w[i], b.w[j]);
+            lo += p[i + j];
+            hi += lo < p[i + j];
+            lo += carry;
+            hi += lo < carry;
+            p[i + j] = lo;
+            carry = hi;
+        }
+        p[i + NL] = carry;
+    }
+    Fx<NL> r;
+SID_ACOS_UNROLL
+    for(int k = 0; k < NL; ++k) r.w[k] = (p[NL - 1 + k] >> 61) | (p[NL + k] << 3);
+    return r;
+}
+
+// Right shift by s bits, 0 < s < 64 (truncating).
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_shr(const Fx<NL>& a, int s) {
+    Fx<NL> r;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) {
+        std::uint64_t hi = i + 1 < NL ? a.w[i + 1] : 0;
+        r.w[i] = (a.w[i] >> s) | (hi << (64 - s));
+    }
+    return r;
+}
+
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_shl1(const Fx<NL>& a) {
+    Fx<NL> r;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) r.w[i] = (a.w[i] << 1) | (i > 0 ? a.w[i - 1] >> 63 : 0);
+    return r;
+}
+
+// A non-negative double below 8, truncated to the format (exact when its last bit is >= 1 unit).
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_from_double(double x) {
+    std::uint64_t b = bits_of(x);
+    int be = static_cast<int>((b >> 52) & 0x7ff);
+    Fx<NL> r = fx_zero<NL>();
+    if(be == 0) return r;   // zero or subnormal: below one unit
+    std::uint64_t m = (b & ((std::uint64_t(1) << 52) - 1)) | (std::uint64_t(1) << 52);
+    int s = be - 1075 + (64 * NL - 3);   // bit position of the mantissa's last bit
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) {
+        int d = s - 64 * i;
+        if(d >= 0) r.w[i] = d < 64 ? m << d : 0;
+        else r.w[i] = d > -64 ? m >> -d : 0;
+    }
+    return r;
+}
+
+template<int NL> struct Terms;
+template<> struct Terms<2> { static constexpr int count = 64; static constexpr int newton = 2; };
+template<> struct Terms<4> { static constexpr int count = 128; static constexpr int newton = 3; };
+
+// asin(t) for t <= 1/2 (plus rounding slack).
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_asin(const Fx<NL>& t) {
+    Fx<NL> t2 = fx_mul(t, t);
+    Fx<NL> s = fx_row<NL>(Terms<NL>::count - 1);
+    for(int k = Terms<NL>::count - 2; k >= 0; --k) s = fx_add(fx_row<NL>(k), fx_mul(s, t2));
+    return fx_mul(t, s);
+}
+
+// sqrt(w) for a double w in [0, 1/4).
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_sqrt_small(double w) {
+    if(w == 0.0) return fx_zero<NL>();
+    int k = static_cast<int>((bits_of(w) >> 52) & 0x7ff) - 1023;   // w = f 2^k, f in [1, 2), k <= -3
+    int e = (k & 1) ? (-1 - k) / 2 : (-2 - k) / 2;                  // m = w 4^e in [1/4, 1), 1 <= e <= 26
+    double m = w * double_of(static_cast<std::uint64_t>(1023 + 2 * e) << 52);
+    Fx<NL> mm = fx_from_double<NL>(m);
+    Fx<NL> y = fx_from_double<NL>(rsqrt_start(m));
+    const Fx<NL> three = fx_int<NL>(3);
+SID_ACOS_UNROLL
+    for(int it = 0; it < Terms<NL>::newton; ++it) {
+        Fx<NL> c = fx_mul(fx_mul(mm, y), y);
+        y = fx_shr(fx_mul(y, fx_sub(three, c)), 1);
+    }
+    return fx_shr(fx_mul(mm, y), e);
+}
+
+// acos(x) for -1 <= x < 1, within 19 units.
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_acos(double x) {
+    double ax = double_of(bits_of(x) & ~(std::uint64_t(1) << 63));
+    bool neg = (bits_of(x) >> 63) != 0;
+    if(ax <= 0.5) {
+        Fx<NL> a = fx_asin(fx_from_double<NL>(ax));
+        Fx<NL> h = fx_row<NL>(kRowPiHalf);
+        return neg ? fx_add(h, a) : fx_sub(h, a);
+    }
+    Fx<NL> a2 = fx_shl1(fx_asin(fx_sqrt_small<NL>((1.0 - ax) * 0.5)));
+    return neg ? fx_sub(fx_row<NL>(kRowPi), a2) : a2;
+}
+
+// The largest floating-point number with `digits` significant bits that is <= v (v > 0), as
+// (significand, exponent of its leading bit relative to the format's units).
+template<int NL> SID_ACOS_HD inline void fx_floor_fp(const Fx<NL>& v, int digits, std::uint64_t& mant, int& lead) {
+    int p = -1;
+SID_ACOS_UNROLL
+    for(int i = NL - 1; i >= 0; --i) {
+        if(p < 0 && v.w[i] != 0) p = 64 * i + 63 - clz64(v.w[i]);
+    }
+    int q = p - digits + 1;   // position of the last kept bit (>= 0: values here are >= 2^-31)
+    std::uint64_t win = 0;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) {
+        int d = 64 * i - q;
+        if(d >= 0) win |= d < 64 ? v.w[i] << d : 0;
+        else win |= d > -64 ? v.w[i] >> -d : 0;
+    }
+    mant = win;
+    lead = p;
+}
+
+// Downward rounding of acos(x) for -1 <= x < 1 at `digits` bits; false if NL limbs cannot decide
+// it (then mant/lead describe the floor of the enclosure's lower end and mant_hi/lead_hi its upper).
+template<int NL> SID_ACOS_HD inline bool acos_floor(double x, int digits, std::uint64_t& mant, int& lead,
+                                                    std::uint64_t& mant_hi, int& lead_hi) {
+    Fx<NL> r = fx_acos<NL>(x);
+    Fx<NL> err = fx_units<NL>(kErrUnits);
+    Fx<NL> lo = fx_less(err, r) ? fx_sub(r, err) : fx_units<NL>(1);
+    Fx<NL> hi = fx_add(r, err);
+    fx_floor_fp(lo, digits, mant, lead);
+    fx_floor_fp(hi, digits, mant_hi, lead_hi);
+    return mant == mant_hi && lead == lead_hi;
+}
+
+// acos(x) rounded down (up = false) or up (up = true) to double (digits 53) or float (digits 24),
+// as bit patterns. NaN and arguments outside [-1, 1] give NaN; acos(1) = +0.
+template<int DIGITS> SID_ACOS_HD SID_ACOS_NOINLINE std::uint64_t acos_rounded_bits(double x, bool up) {
+    constexpr int kFrac2 = 64 * 2 - 3, kFrac4 = 64 * 4 - 3;
+    constexpr int kBias = DIGITS == 53 ? 1023 : 127;
+    constexpr std::uint64_t kNaN = DIGITS == 53 ? 0x7ff8000000000000ull : 0x7fc00000ull;
+    if(!(x >= -1.0 && x <= 1.0)) return kNaN;
+    if(x == 1.0) return 0;
+    std::uint64_t mant, mant_hi;
+    int lead, lead_hi, frac = kFrac2;
+    if(!acos_floor<2>(x, DIGITS, mant, lead, mant_hi, lead_hi)) {
+        frac = kFrac4;
+        if(!acos_floor<4>(x, DIGITS, mant, lead, mant_hi, lead_hi) && up) {
+            mant = mant_hi;   // undecided even with four limbs: outward enclosure
+            lead = lead_hi;
+        }
+    }
+    std::uint64_t b = (static_cast<std::uint64_t>(lead - frac + kBias) << (DIGITS - 1)) |
+                      (mant & ((std::uint64_t(1) << (DIGITS - 1)) - 1));
+    return up ? b + 1 : b;   // the successor of a positive number: next bit pattern
+}
+
+SID_ACOS_HD inline double acos_rd(double x) { return double_of(acos_rounded_bits<53>(x, false)); }
+SID_ACOS_HD inline double acos_ru(double x) { return double_of(acos_rounded_bits<53>(x, true)); }
+SID_ACOS_HD inline float acos_rd(float x) {
+    return float_of(static_cast<std::uint32_t>(acos_rounded_bits<24>(x, false)));
+}
+SID_ACOS_HD inline float acos_ru(float x) {
+    return float_of(static_cast<std::uint32_t>(acos_rounded_bits<24>(x, true)));
+}
+
+} // namespace acos_cr
+
+#if defined(__CUDACC__)
+// Interval arc cosine: clamp to [-1, 1] (marking the result possibly undefined) only where the
+// argument's compile-time bounds leave the domain, as the reference does.
+template<class T, bool CLAMP_LO, bool CLAMP_HI> __device__ inline Iv<T> iv_acos(Iv<T> x) {
+    bool und = x.und;
+    if(CLAMP_LO && x.lo < T(-1)) {
+        und = true;
+        x.lo = T(-1);
+    }
+    if(CLAMP_HI && T(1) < x.hi) {
+        und = true;
+        x.hi = T(1);
+    }
+    return {acos_cr::acos_rd(x.hi), acos_cr::acos_ru(x.lo), und};
+}
+#endif
+
+} // namespace sid
