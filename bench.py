@@ -11,8 +11,10 @@ of the prover core. Inputs (805 MB) and outputs exceed the 129 MB L2, so no flus
 
 value: cuboids/s with the batch resident in HBM (CUDA events on the launching stream, max over ranks).
 e2e: the same through the C ABI with host buffers (sid_eval_batch: H2D copy, kernel, D2H copy).
-Extra fields: the full One Subcontainer proof on the GPU, the roofline of the batch kernel, the CPU
-oracle (a restatement of the reference's CPU prover) timed on the host cores.
+Extra fields: the full One Subcontainer proof on the GPU; every lemma proved in the plain FP64 form and
+in the precision form (FP32 first pass, FP64 escalation) with cuboids/s, escalation rate and count change
+(lemma_set); the roofline of the batch kernel; the CPU oracle (a restatement of the reference's CPU
+prover) timed on the host cores.
 --impl reference times the reference's CPU algorithm (the oracle port; the reference itself cannot be
 built on the GPU machine) on the same workload with all host threads.
 """
@@ -127,6 +129,44 @@ def cpu_baseline(ir, lo, hi, threads, budget_s=1.5):
     oracle_py.eval_batch(ir, lo[:, :sample], hi[:, :sample], threads=threads)
     dt = time.perf_counter() - t0
     return sample, dt
+
+
+PRECISION_PLAIN, PRECISION_FP32 = 0, 1
+PUBLISHED = os.path.join(REPO, "tests", "golden", "published_counts.json")
+
+
+def prove_lemma_set(eng, sid, repeats=2):
+    """Every lemma proved on this GPU in the plain FP64 form and in the precision form (FP32 first pass,
+    FP64 for the children FP32 cannot refute): best-of-`repeats` device time, cuboids/s, the escalation
+    rate and the count change against the reference's published counts."""
+    with open(PUBLISHED) as f:
+        published = json.load(f)
+    out = {}
+    tot = {"plain_s": 0.0, "fp32_s": 0.0, "cuboids": 0}
+    for name in sid.lemma_names():
+        lid = eng.register(sid.lemma_ir(name))
+        row = {"published": published.get(name)}
+        for key, prec in (("plain", PRECISION_PLAIN), ("fp32", PRECISION_FP32)):
+            runs = [eng.prove(lid, precision=prec) for _ in range(repeats)]
+            r = min(runs, key=lambda x: x["seconds"])
+            row[key] = {"cuboids": r["cuboids"], "leaves": r["leaves"], "criticals": r["criticals"],
+                        "seconds": r["seconds"], "cuboids_per_s": r["cuboids"] / max(r["seconds"], 1e-9)}
+            if prec == PRECISION_FP32:
+                row[key]["escalated"] = r["escalated"]
+                row[key]["escalation_rate"] = r["escalated"] / max(r["cuboids"], 1)
+        pub = published.get(name) or [None, None]
+        row["delta_cuboids_fp32_vs_published"] = None if pub[0] is None else row["fp32"]["cuboids"] - pub[0]
+        row["plain_matches_published"] = [row["plain"]["cuboids"], row["plain"]["leaves"]] == pub
+        row["speedup_fp32_vs_plain"] = row["plain"]["seconds"] / max(row["fp32"]["seconds"], 1e-9)
+        tot["plain_s"] += row["plain"]["seconds"]
+        tot["fp32_s"] += row["fp32"]["seconds"]
+        tot["cuboids"] += row["plain"]["cuboids"]
+        out[name] = row
+    out["_total"] = {"cuboids": tot["cuboids"], "plain_seconds": tot["plain_s"], "fp32_seconds": tot["fp32_s"],
+                     "plain_cuboids_per_s": tot["cuboids"] / max(tot["plain_s"], 1e-9),
+                     "fp32_cuboids_per_s": tot["cuboids"] / max(tot["fp32_s"], 1e-9),
+                     "speedup_fp32_vs_plain": tot["plain_s"] / max(tot["fp32_s"], 1e-9)}
+    return out
 
 
 def run_reference(args):
@@ -248,6 +288,7 @@ def run_ours(args):
     eng.prove(lid)
     proofs = [eng.prove(lid) for _ in range(3)]
     best = min(proofs, key=lambda r: r["seconds"])
+    lemma_set = prove_lemma_set(eng, sid) if not args.no_lemma_set else None
 
     if rank != 0:
         return 0
@@ -273,6 +314,8 @@ def run_ours(args):
                   "criticals": best["criticals"], "seconds": best["seconds"],
                   "cuboids_per_s": best["cuboids"] / best["seconds"]},
     }
+    if lemma_set:
+        line["lemma_set"] = lemma_set
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sample, dt = cpu_baseline(ir, lo, hi, threads)
@@ -292,6 +335,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-lemma-set", action="store_true", help="skip the full-proof lemma set")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -60,7 +60,12 @@ typedef struct sid_progress {
 typedef void (*sid_progress_fn)(void* user, const sid_progress* progress);
 
 #define SID_PRECISION_PLAIN 0           /* the lemma's own number type, bit-exact with the reference */
-#define SID_PRECISION_FP32_ESCALATE 1   /* FP32 first pass, undecided cuboids re-checked in FP64 */
+#define SID_PRECISION_FP32_ESCALATE 1   /* precision form for double lemmas: every child cuboid is first
+                                           propagated and tested in FP32 (outward rounded, sound); only
+                                           the children FP32 cannot refute are evaluated in FP64, whose
+                                           results are used. Counts equal the plain form's unless FP32
+                                           refutes a child FP64 would not (possible only through a
+                                           different propagation order); float lemmas run plain. */
 
 /* Settings of one proof; meaning as ivarp::ProverSettings (prover_input.hpp:124-159). */
 typedef struct sid_prove_opts {

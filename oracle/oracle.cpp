@@ -13,9 +13,11 @@
 #include <condition_variable>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <thread>
+#include <type_traits>
 
 namespace sido {
 namespace {
@@ -462,6 +464,16 @@ template<class T> struct Prover {
     bool all_ok(const Iv<T>* box) { return rows_ok(L.nargs - 1, L.nargs, box); }
 };
 
+/// The provers one worker uses: the lemma's own number type, and for double lemmas in the precision form
+/// a float prover that tries to refute each child first.
+template<class T> struct Provers {
+    Prover<T> P;
+    std::unique_ptr<Prover<float>> F;
+    Provers(const LemmaIR& l, bool fp32_first) : P(l) {
+        if(fp32_first && std::is_same<T, double>::value) F.reset(new Prover<float>(l));
+    }
+};
+
 template<class T> inline void split_point_pair(T lb, T ub, int n, int i, T& lo, T& hi) {
     T w = (ub - lb) / T(n);
     lo = (i >= n) ? ub : lb + T(i) * w;
@@ -505,18 +517,35 @@ template<class T> struct Driver {
 
     Driver(const LemmaIR& l, const ProveOptions& o) : L(l), opt(o), dyn(l.dynamic_splits()), stat(l.static_splits()) {}
 
-    void init(Prover<T>& P, Counts& c) {
+    void init(Provers<T>& S, Counts& c) {
         std::vector<Iv<T>> root = initial_box<T>(L);
         const std::size_t n = std::size_t(L.nargs);
         const unsigned rec_limit = unsigned(std::min<std::size_t>(n, 255));
         std::vector<Element<T>> out;
         std::vector<Iv<T>> cur = root;
-        init_rec(P, c, 0, cur, rec_limit, out);
+        init_rec(S, c, 0, cur, rec_limit, out);
         queue = std::move(out);
     }
 
-    void init_rec(Prover<T>& P, Counts& c, std::size_t d, const std::vector<Iv<T>>& box, unsigned rec_limit,
+    /// Precision form: true if the float evaluation of this child (its box rounded outward to float,
+    /// then the same propagation and constraint rows as the double path) already refutes it.
+    bool refuted_in_fp32(Provers<T>& S, Counts& c, const std::vector<Iv<T>>& child, int arg, std::size_t it,
+                         unsigned rec, int r0, int r1) {
+        if(!S.F) return false;
+        std::vector<Iv<float>>& fb = fbox;
+        fb.resize(child.size());
+        for(std::size_t v = 0; v < child.size(); ++v) {
+            fb[v] = {static_cast<float>(child[v].lo), -static_cast<float>(-child[v].hi), false};   // round-down mode
+        }
+        bool refuted = S.F->propagate(arg, fb.data(), it, rec) || (r1 > r0 && !S.F->rows_ok(r0, r1, fb.data()));
+        if(refuted) ++c.fp32_refuted; else ++c.escalated;
+        return refuted;
+    }
+    static thread_local std::vector<Iv<float>> fbox;
+
+    void init_rec(Provers<T>& S, Counts& c, std::size_t d, const std::vector<Iv<T>>& box, unsigned rec_limit,
                   std::vector<Element<T>>& out) {
+        Prover<T>& P = S.P;
         if(d == dyn.size()) {
             if(P.all_ok(box.data())) out.push_back({box, 0}); else ++c.leaves;
             return;
@@ -529,8 +558,10 @@ template<class T> struct Driver {
             T lo, hi;
             split_point_pair(box[std::size_t(s.arg)].lo, box[std::size_t(s.arg)].hi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
+            if(refuted_in_fp32(S, c, child, s.arg, 2 * std::size_t(L.nargs), rec_limit, d + 1 == dyn.size() ? L.nargs - 1 : 0,
+                               d + 1 == dyn.size() ? L.nargs : 0)) { ++c.leaves; continue; }
             if(P.propagate(s.arg, child.data(), 2 * L.nargs, rec_limit)) { ++c.leaves; continue; }
-            init_rec(P, c, d + 1, child, rec_limit, out);
+            init_rec(S, c, d + 1, child, rec_limit, out);
         }
     }
 
@@ -540,7 +571,8 @@ template<class T> struct Driver {
     };
 
     /// Static-split recursion (CPUProverCore::p_handle_cuboid).
-    void handle(Prover<T>& P, Counts& c, std::size_t j, std::vector<Iv<T>>& box, Hull* hull) {
+    void handle(Provers<T>& S, Counts& c, std::size_t j, std::vector<Iv<T>>& box, Hull* hull) {
+        Prover<T>& P = S.P;
         if(j == stat.size()) {
             ++c.leaves;
             if(hull) {
@@ -571,9 +603,10 @@ template<class T> struct Driver {
             T lo, hi;
             split_point_pair(plo, phi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
+            if(refuted_in_fp32(S, c, child, s.arg, std::size_t(L.nargs), 4, r0, r1)) { ++c.leaves; continue; }
             if(P.propagate(s.arg, child.data(), std::size_t(L.nargs), 4)) { ++c.leaves; continue; }
             if(!P.rows_ok(r0, r1, child.data())) { ++c.leaves; continue; }
-            handle(P, c, j + 1, child, hull);
+            handle(S, c, j + 1, child, hull);
         }
         c.cuboids += std::uint64_t(m);
     }
@@ -593,8 +626,9 @@ template<class T> struct Driver {
     }
 
     /// Dynamic re-split of a hull (SplitIntoImpl::perform_split).
-    void split_rec(Prover<T>& P, Counts& c, std::size_t d, const std::vector<Iv<T>>& box, unsigned depth,
+    void split_rec(Provers<T>& S, Counts& c, std::size_t d, const std::vector<Iv<T>>& box, unsigned depth,
                    std::vector<Element<T>>& out) {
+        Prover<T>& P = S.P;
         if(d == dyn.size()) {
             if(P.all_ok(box.data())) out.push_back({box, depth}); else ++c.leaves;
             return;
@@ -608,22 +642,24 @@ template<class T> struct Driver {
             T lo, hi;
             split_point_pair(box[std::size_t(s.arg)].lo, box[std::size_t(s.arg)].hi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
+            if(refuted_in_fp32(S, c, child, s.arg, 2 * std::size_t(L.nargs), rec_limit, d + 1 == dyn.size() ? L.nargs - 1 : 0,
+                               d + 1 == dyn.size() ? L.nargs : 0)) { ++c.leaves; continue; }
             if(P.propagate(s.arg, child.data(), 2 * L.nargs, rec_limit)) { ++c.leaves; continue; }
-            split_rec(P, c, d + 1, child, depth, out);
+            split_rec(S, c, d + 1, child, depth, out);
         }
     }
 
-    void process(Prover<T>& P, Counts& c, Element<T> e, std::vector<Element<T>>& out) {
+    void process(Provers<T>& S, Counts& c, Element<T> e, std::vector<Element<T>>& out) {
         int it = 0;
         for(;;) {
             Hull h;
-            handle(P, c, 0, e.box, &h);
+            handle(S, c, 0, e.box, &h);
             if(h.empty) return;
             if(++it >= opt.max_iterations || !should_iterate(h.box, e.box)) {
                 if(e.depth >= opt.generations) {
-                    handle(P, c, 0, h.box, nullptr);
+                    handle(S, c, 0, h.box, nullptr);
                 } else {
-                    split_rec(P, c, 0, h.box, e.depth + 1, out);
+                    split_rec(S, c, 0, h.box, e.depth + 1, out);
                 }
                 return;
             }
@@ -636,7 +672,7 @@ template<class T> struct Driver {
     void worker() {
         try {
             RoundDownScope rd;
-            Prover<T> P(L);
+            Provers<T> S(L, opt.fp32_first);
             Counts c;
             std::vector<Element<T>> batch, out;
             for(;;) {
@@ -650,7 +686,7 @@ template<class T> struct Driver {
                     ++busy;
                 }
                 out.clear();
-                for(auto& e : batch) process(P, c, std::move(e), out);
+                for(auto& e : batch) process(S, c, std::move(e), out);
                 {
                     std::lock_guard<std::mutex> lk(mtx);
                     for(auto& e : out) queue.push_back(std::move(e));
@@ -671,9 +707,9 @@ template<class T> struct Driver {
         auto t0 = std::chrono::steady_clock::now();
         {
             RoundDownScope rd;
-            Prover<T> P(L);
+            Provers<T> S(L, opt.fp32_first);
             Counts c;
-            init(P, c);
+            init(S, c);
             total += c;
         }
         int nt = opt.threads > 0 ? opt.threads : int(std::max(1u, std::thread::hardware_concurrency()));
@@ -690,6 +726,8 @@ template<class T> struct Driver {
 
     std::mutex crit_mtx;
 };
+
+template<class T> thread_local std::vector<Iv<float>> Driver<T>::fbox;
 
 } // namespace
 

@@ -41,8 +41,10 @@ namespace sido {
 
 struct Counts {
     std::uint64_t cuboids = 0, leaves = 0, criticals = 0, repeated = 0;
+    std::uint64_t fp32_refuted = 0, escalated = 0;   // precision form: children decided in float / passed on
     Counts& operator+=(const Counts& o) {
         cuboids += o.cuboids; leaves += o.leaves; criticals += o.criticals; repeated += o.repeated;
+        fp32_refuted += o.fp32_refuted; escalated += o.escalated;
         return *this;
     }
 };
@@ -54,6 +56,9 @@ struct ProveOptions {
     float iteration_single = 0.66f;
     int threads = 0;                 // 0: hardware concurrency
     std::uint64_t max_criticals = 0; // criticals stored
+    bool fp32_first = false;         // precision form (double lemmas): children are first evaluated in
+                                     // float, rounded outward; only those float cannot refute are
+                                     // evaluated in double, whose results are used
 };
 
 struct ProveResult {

@@ -15,13 +15,15 @@ extern "C" {
 
 const char* sido_last_error(void) { return last_error.c_str(); }
 
-/* counts_out: cuboids, leaves, criticals, repeated. crit_out may be NULL; it receives up to crit_cap
- * criticals (2*nargs doubles each); *crit_n receives the number of stored (lo,hi) pairs. */
+/* counts_out: cuboids, leaves, criticals, repeated, fp32_refuted, escalated. crit_out may be NULL; it
+ * receives up to crit_cap criticals (2*nargs doubles each); *crit_n receives the number of stored (lo,hi)
+ * pairs. fp32_first selects the precision form. */
 int sido_prove(const char* ir, unsigned generations, int max_iterations, float vol, float single, int threads,
-               unsigned long long* counts_out, double* seconds, double* crit_out, unsigned long long crit_cap,
-               unsigned long long* crit_n) {
+               int fp32_first, unsigned long long* counts_out, double* seconds, double* crit_out,
+               unsigned long long crit_cap, unsigned long long* crit_n) {
     try {
         sido::ProveOptions o;
+        o.fp32_first = fp32_first != 0;
         o.generations = generations;
         o.max_iterations = max_iterations;
         o.iteration_volume = vol;
@@ -33,6 +35,8 @@ int sido_prove(const char* ir, unsigned generations, int max_iterations, float v
         counts_out[1] = r.counts.leaves;
         counts_out[2] = r.counts.criticals;
         counts_out[3] = r.counts.repeated;
+        counts_out[4] = r.counts.fp32_refuted;
+        counts_out[5] = r.counts.escalated;
         if(seconds) *seconds = r.seconds;
         if(crit_out && !r.criticals.empty()) {
             std::memcpy(crit_out, r.criticals.data(), r.criticals.size() * sizeof(double));

@@ -26,7 +26,8 @@ def lib():
         _lib = ctypes.CDLL(LIB)
         _lib.sido_prove.restype = ctypes.c_int
         _lib.sido_prove.argtypes = [ctypes.c_char_p, ctypes.c_uint, ctypes.c_int, ctypes.c_float, ctypes.c_float,
-                                    ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong),
+                                    ctypes.POINTER(ctypes.c_double),
                                     ctypes.c_void_p, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)]
         _lib.sido_root_box.restype = ctypes.c_int
         _lib.sido_root_box.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
@@ -43,10 +44,11 @@ def _err():
     return lib().sido_last_error().decode()
 
 
-def prove(ir_text, generations=8, max_iterations=1, threads=0, max_criticals=0, nargs=None):
-    """Run the oracle proof; returns dict(cuboids, leaves, criticals, repeated, seconds, boxes)."""
+def prove(ir_text, generations=8, max_iterations=1, threads=0, max_criticals=0, nargs=None, fp32_first=False):
+    """Run the oracle proof; returns dict(cuboids, leaves, criticals, repeated, fp32_refuted, escalated, seconds,
+    boxes). fp32_first selects the precision form (float first, double for what float cannot refute)."""
     L = lib()
-    counts = (ctypes.c_ulonglong * 4)()
+    counts = (ctypes.c_ulonglong * 6)()
     secs = ctypes.c_double()
     n_pairs = ctypes.c_ulonglong(0)
     buf = None
@@ -54,11 +56,13 @@ def prove(ir_text, generations=8, max_iterations=1, threads=0, max_criticals=0, 
         if nargs is None:
             nargs = int([l for l in ir_text.splitlines() if l.startswith("nargs ")][0].split()[1])
         buf = np.zeros(max_criticals * 2 * nargs, dtype=np.float64)
-    rc = L.sido_prove(ir_text.encode(), generations, max_iterations, 0.25, 0.66, threads, counts, ctypes.byref(secs),
+    rc = L.sido_prove(ir_text.encode(), generations, max_iterations, 0.25, 0.66, threads, 1 if fp32_first else 0,
+                      counts, ctypes.byref(secs),
                       buf.ctypes.data if buf is not None else None, max_criticals, ctypes.byref(n_pairs))
     if rc != 0:
         raise RuntimeError("oracle: " + _err())
-    out = dict(cuboids=counts[0], leaves=counts[1], criticals=counts[2], repeated=counts[3], seconds=secs.value)
+    out = dict(cuboids=counts[0], leaves=counts[1], criticals=counts[2], repeated=counts[3], fp32_refuted=counts[4],
+               escalated=counts[5], seconds=secs.value)
     if buf is not None:
         out["boxes"] = buf[: n_pairs.value * 2].reshape(-1, nargs, 2)
     return out

@@ -354,12 +354,18 @@ def generate(lemma):
     w("static cudaError_t level(int mode, const LevelArgs& a, cudaStream_t s) { return launch_level<L, %s>(mode, a, s); }" % T_plain)
     w("static cudaError_t root_box(double2* o, cudaStream_t s) { return launch_root_box<L, %s>(o, s); }" % T_plain)
     w("static cudaError_t eval_batch(const BatchArgs& a, cudaStream_t s) { return launch_eval_batch<L, %s>(a, s); }" % T_plain)
+    if L.numtype != "f32":
+        w("static cudaError_t filter_f32(const LevelArgs& a, cudaStream_t s) { return launch_filter_f32<L>(a, s); }")
+        w("static cudaError_t level_esc(int mode, const LevelArgs& a, unsigned blocks, cudaStream_t s) {")
+        w("    return launch_level_esc<L>(mode, a, blocks, s);")
+        w("}")
     w("")
     w("} // namespace %s" % ns)
     w("")
     w("extern const LemmaKernels kernels_%s;" % ns)
-    w("const LemmaKernels kernels_%s = {\"%s\", 0x%016xull, %d, %d, %s, &%s::level, &%s::root_box, &%s::eval_batch};" % (
-        ns, L.slug, L.fingerprint, L.nargs, len(L.bounds), "true" if L.numtype == "f32" else "false", ns, ns, ns))
+    prec = "nullptr, nullptr" if L.numtype == "f32" else "&%s::filter_f32, &%s::level_esc" % (ns, ns)
+    w("const LemmaKernels kernels_%s = {\"%s\", 0x%016xull, %d, %d, %s, &%s::level, &%s::root_box, &%s::eval_batch, %s};" % (
+        ns, L.slug, L.fingerprint, L.nargs, len(L.bounds), "true" if L.numtype == "f32" else "false", ns, ns, ns, prec))
     w("")
     w("} // namespace sid")
     return ns, "\n".join(out) + "\n"

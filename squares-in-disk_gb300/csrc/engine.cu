@@ -121,6 +121,7 @@ struct BoxList {
 struct Lemma {
     sid::LemmaIR ir;
     const sid::LemmaKernels* k = nullptr;
+    DevBuf<double2> root;                // initial runtime box, computed once at registration
     std::vector<double> criticals;       // from the last proof
 };
 
@@ -131,11 +132,13 @@ struct sid_engine {
     cudaStream_t stream = nullptr;
     std::vector<std::unique_ptr<Lemma>> lemmas;
     // scratch reused across proofs
+    int sm_count = 0;
     DevBuf<unsigned long long> counters;   // [0] leaves [1] criticals [2] out_count [3] fin [4] nf
+                                           // [5] escalation list length [6] escalated in total
     DevBuf<unsigned int> overflow;
+    DevBuf<std::uint32_t> esc;             // precision form: escalation list of one chunk of children
     DevBuf<unsigned long long> hull;       // 4 * batch * nargs
     DevBuf<double> crit;
-    DevBuf<double2> root;
     BoxList queue, fin, nonfin;
     std::vector<std::unique_ptr<BoxList>> stat_levels, dyn_levels;
     DevBuf<double> batch_in_lo, batch_in_hi, batch_out_lo, batch_out_hi;
@@ -220,6 +223,8 @@ using namespace sid;
 
 constexpr std::uint64_t kLevelCapItems = std::uint64_t(8) << 20;   // items per intermediate level list
 constexpr std::uint64_t kDefaultBatch = std::uint64_t(1) << 16;    // queue elements per step
+constexpr std::uint64_t kEscChunk = std::uint64_t(1) << 24;        // children per precision-form pass pair
+constexpr unsigned kEscBlocksPerSM = 8;                            // grid of the escalated (double) pass
 
 struct Prover {
     sid_engine* eng;
@@ -237,12 +242,16 @@ struct Prover {
     unsigned long long* d_nf = nullptr;
     std::uint64_t crit_cap = 0;
     std::uint64_t host_leaves = 0;     // leaves counted on the host (lemmas without static splits)
+    bool fp32_first = false;           // precision form
+    unsigned long long* d_esc = nullptr;
+    unsigned long long* d_esc_total = nullptr;
 
     Prover(sid_engine* e, Lemma* l, const sid_prove_opts& o) : eng(e), lem(l), opts(o) {
         n = l->ir.nargs;
         dyn = l->ir.dynamic_splits();
         stat = l->ir.static_splits();
         if(o.batch_elements > 0) batch = std::uint64_t(o.batch_elements);
+        fp32_first = o.precision == SID_PRECISION_FP32_ESCALATE && l->k->filter_f32 != nullptr;
     }
 
     cudaStream_t s() const { return eng->stream; }
@@ -268,9 +277,27 @@ struct Prover {
         return a;
     }
 
-    void launch(int mode, const LevelArgs& a) {
-        cuda_check(lem->k->level(mode, a, s()), "level kernel launch");
-        cuboids += a.n_in * std::uint64_t(a.nsub);
+    void launch(int mode, const LevelArgs& a0) {
+        const std::uint64_t total = a0.n_in * std::uint64_t(a0.nsub);
+        cuboids += total;
+        if(!fp32_first) {
+            cuda_check(lem->k->level(mode, a0, s()), "level kernel launch");
+            return;
+        }
+        // precision form: float pass over a chunk of children, then double pass over its escalation list
+        for(std::uint64_t cb = 0; cb < total; cb += kEscChunk) {
+            LevelArgs a = a0;
+            a.child_begin = cb;
+            a.n_child = std::min(kEscChunk, total - cb);
+            a.esc = eng->esc.p;
+            a.esc_count = d_esc;
+            a.esc_total = d_esc_total;
+            cuda_check(cudaMemsetAsync(d_esc, 0, sizeof(unsigned long long), s()), "reset escalation count");
+            cuda_check(lem->k->filter_f32(a, s()), "float pass launch");
+            const std::uint64_t want = (a.n_child + 127) / 128;
+            const unsigned blocks = unsigned(std::min<std::uint64_t>(want, std::uint64_t(eng->sm_count) * kEscBlocksPerSM));
+            cuda_check(lem->k->level_esc(mode, a, blocks, s()), "escalated pass launch");
+        }
     }
 
     BoxList& stat_level(std::size_t j) {
@@ -443,12 +470,14 @@ struct Prover {
         eng->overflow.reserve(1);
         eng->hull.reserve(4 * batch * std::uint64_t(n));
         eng->crit.reserve(std::max<std::uint64_t>(1, crit_cap) * 2 * std::uint64_t(n));
-        eng->root.reserve(std::size_t(n));
         d_leaf = eng->counters.p;
         d_crit = eng->counters.p + 1;
         d_out = eng->counters.p + 2;
         d_fin = eng->counters.p + 3;
         d_nf = eng->counters.p + 4;
+        d_esc = eng->counters.p + 5;
+        d_esc_total = eng->counters.p + 6;
+        if(fp32_first) eng->esc.reserve(kEscChunk);
         cuda_check(cudaMemsetAsync(eng->counters.p, 0, 8 * sizeof(unsigned long long), s()), "memset counters");
         cuda_check(cudaMemsetAsync(eng->overflow.p, 0, sizeof(unsigned int), s()), "memset overflow");
         eng->fin.reserve(n, batch, false, false, true);
@@ -464,10 +493,9 @@ struct Prover {
         auto last_cb = t0;
         bool first_done = false;
 
-        // root box and root partition
-        cuda_check(lem->k->root_box(eng->root.p, s()), "root box");
+        // root partition of the lemma's initial runtime box
         queue_reserve(1 << 16);
-        run_dynamic(0, eng->root.p, 1, nullptr, 0, 1, true, 0);
+        run_dynamic(0, lem->root.p, 1, nullptr, 0, 1, true, 0);
 
         while(qsize > 0) {
             const std::uint64_t B = std::min(qsize, batch);
@@ -541,7 +569,7 @@ struct Prover {
         res->num_critical_cuboids = read_counter(d_crit);
         res->num_repeated_nodes = 0;
         res->criticals_stored = std::min<std::uint64_t>(res->num_critical_cuboids, crit_cap);
-        res->escalated = 0;
+        res->escalated = fp32_first ? read_counter(d_esc_total) : 0;
         res->seconds = double(ms) / 1000.0;
         lem->criticals.assign(std::size_t(res->criticals_stored) * 2 * std::size_t(n), 0.0);
         if(res->criticals_stored) {
@@ -611,6 +639,7 @@ int sid_engine_create(int device, sid_engine** out) {
         auto e = std::make_unique<sid_engine>();
         e->device = device;
         set_device(e.get());
+        cuda_check(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");
         cuda_check(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         *out = e.release();
     });
@@ -645,6 +674,12 @@ int sid_lemma_register(sid_engine* engine, const char* ir, size_t ir_len, int* l
         for(std::size_t i = 0; i < engine->lemmas.size(); ++i) {
             if(engine->lemmas[i]->ir.fingerprint == lem->ir.fingerprint) { *lemma_id = int(i); return; }
         }
+        // initial runtime bounds, once per lemma (the reference computes them when building its
+        // prover input, refactor_constraints_impl.hpp:90-101)
+        set_device(engine);
+        lem->root.reserve(std::size_t(lem->ir.nargs));
+        cuda_check(lem->k->root_box(lem->root.p, engine->stream), "root box");
+        cuda_check(cudaStreamSynchronize(engine->stream), "root box sync");
         engine->lemmas.push_back(std::move(lem));
         *lemma_id = int(engine->lemmas.size() - 1);
     });
@@ -663,9 +698,7 @@ int sid_lemma_root_box(sid_engine* engine, int lemma_id, double* out_lohi) {
         Lemma* l = get_lemma(engine, lemma_id);
         if(!out_lohi) fail(SID_ERR_INVALID, "null output");
         set_device(engine);
-        engine->root.reserve(std::size_t(l->ir.nargs));
-        cuda_check(l->k->root_box(engine->root.p, engine->stream), "root box");
-        cuda_check(cudaMemcpyAsync(out_lohi, engine->root.p, sizeof(double2) * std::size_t(l->ir.nargs),
+        cuda_check(cudaMemcpyAsync(out_lohi, l->root.p, sizeof(double2) * std::size_t(l->ir.nargs),
                                    cudaMemcpyDeviceToHost, engine->stream), "root box copy");
         cuda_check(cudaStreamSynchronize(engine->stream), "root box sync");
     });
@@ -677,7 +710,9 @@ int sid_prove(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, sid_
         if(!result) fail(SID_ERR_INVALID, "null result");
         sid_prove_opts o;
         if(opts) o = *opts; else sid_prove_opts_default(&o);
-        if(o.precision != SID_PRECISION_PLAIN) fail(SID_ERR_UNSUPPORTED, "precision mode %d not supported", o.precision);
+        if(o.precision != SID_PRECISION_PLAIN && o.precision != SID_PRECISION_FP32_ESCALATE) {
+            fail(SID_ERR_INVALID, "unknown precision mode %d", o.precision);
+        }
         if(o.generation_count > 250) fail(SID_ERR_INVALID, "generation_count too large");
         set_device(engine);
         std::memset(result, 0, sizeof(*result));

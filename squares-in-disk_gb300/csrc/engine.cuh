@@ -175,19 +175,21 @@ struct LevelArgs {
     // counters
     unsigned long long* leaf_count;
     unsigned int* overflow;           // set when an output list would overflow
+    // precision form (k_filter_f32 / k_level_esc): children [child_begin, child_begin + n_child) of
+    // the items, the escalation list (child ids relative to child_begin) and its length
+    std::uint64_t child_begin, n_child;
+    std::uint32_t* esc;
+    unsigned long long* esc_count;
+    unsigned long long* esc_total;    // escalated children over the whole proof
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
-template<class L, class T, int MODE> __global__ void __launch_bounds__(128) k_level(const LevelArgs a) {
+/// One child c of item `item`: split, propagate, test rows, then emit / join / store. All lanes of
+/// `active` call this together (warp-aggregated atomics).
+template<class L, class T, int MODE>
+__device__ __forceinline__ void level_child(const LevelArgs& a, const std::uint64_t item, const int c, const unsigned active) {
     constexpr int N = L::NARGS;
-    const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
-    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if(t >= total) return;
-    const unsigned active = __activemask();
-    const std::uint64_t item = a.in_begin + t / std::uint64_t(a.nsub);
-    const int c = int(t % std::uint64_t(a.nsub));
-
     Iv<T> box[N];
     #pragma unroll
     for(int v = 0; v < N; ++v) {
@@ -265,6 +267,64 @@ template<class L, class T, int MODE> __global__ void __launch_bounds__(128) k_le
     if(int(lane_id()) == __ffs(active) - 1 && wsum) atomicAdd(a.leaf_count, (unsigned long long)wsum);
 }
 
+template<class L, class T, int MODE> __global__ void __launch_bounds__(128) k_level(const LevelArgs a) {
+    const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
+    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(t >= total) return;
+    const unsigned active = __activemask();
+    level_child<L, T, MODE>(a, a.in_begin + t / std::uint64_t(a.nsub), int(t % std::uint64_t(a.nsub)), active);
+}
+
+/// Precision form, first pass: children [child_begin, child_begin + n_child) of the launch's items
+/// (child id = item offset * nsub + child) are split in double exactly as in the plain form, rounded
+/// outward to float, and propagated and tested in float. A child refuted in float is a leaf (interval
+/// arithmetic in float is as sound as in double); every other child id goes to the escalation list,
+/// whose children are then evaluated in double by k_level_esc, with double results used throughout.
+template<class L> __global__ void __launch_bounds__(128) k_filter_f32(const LevelArgs a) {
+    constexpr int N = L::NARGS;
+    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(t >= a.n_child) return;
+    const unsigned active = __activemask();
+    const std::uint64_t id = a.child_begin + t;
+    const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
+    const int c = int(id % std::uint64_t(a.nsub));
+    Iv<float> box[N];
+    #pragma unroll
+    for(int v = 0; v < N; ++v) {
+        double2 b = a.in_box[std::uint64_t(v) * a.in_stride + item];
+        if(v == a.var) split_child(b.x, b.y, a.nsub, c, b.x, b.y);
+        box[v] = {__double2float_rd(b.x), __double2float_ru(b.y), false};
+    }
+    bool ok = !propagate<L, float>(a.var, box, a.it_limit, a.rec_limit);
+    if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<float>(a.row_begin, a.row_end, box);
+    const unsigned m = __ballot_sync(active, ok);
+    const int leader = __ffs(active) - 1;
+    unsigned long long base = 0;
+    if(int(lane_id()) == leader && m) {
+        base = atomicAdd(a.esc_count, (unsigned long long)__popc(m));
+        atomicAdd(a.esc_total, (unsigned long long)__popc(m));
+    }
+    base = __shfl_sync(active, base, leader);
+    if(ok) a.esc[base + __popc(m & ((1u << lane_id()) - 1u))] = std::uint32_t(t);
+    const unsigned refuted = __popc(active & ~m);
+    if(int(lane_id()) == leader && refuted) atomicAdd(a.leaf_count, (unsigned long long)refuted);
+}
+
+/// Precision form, second pass: the escalated children, in double, with the plain form's outputs.
+/// Grid-stride over the list (its length is read on the device, so no host round trip is needed).
+template<class L, int MODE> __global__ void __launch_bounds__(128) k_level_esc(const LevelArgs a) {
+    const std::uint64_t n = *a.esc_count;
+    const std::uint64_t stride = std::uint64_t(gridDim.x) * blockDim.x;
+    for(std::uint64_t base = std::uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const std::uint64_t j = base + lane_id();
+        const bool valid = j < n;
+        const unsigned active = __ballot_sync(0xffffffffu, valid);
+        if(!valid) continue;   // only in the warp's last round: base + stride >= n
+        const std::uint64_t id = a.child_begin + a.esc[j];
+        level_child<L, double, MODE>(a, a.in_begin + id / std::uint64_t(a.nsub), int(id % std::uint64_t(a.nsub)), active);
+    }
+}
+
 /// Initial runtime box: compile-time bounds (fixed point / 1e6, rounded outward) tightened by 50*nargs
 /// rounds of all bounds in table order (refactor_constraints_impl.hpp:71-101).
 template<class L, class T> __global__ void k_root_box(double2* out) {
@@ -329,6 +389,9 @@ struct LemmaKernels {
     cudaError_t (*level)(int mode, const LevelArgs& a, cudaStream_t s);
     cudaError_t (*root_box)(double2* out, cudaStream_t s);
     cudaError_t (*eval_batch)(const BatchArgs& a, cudaStream_t s);
+    // precision form (double lemmas only; null for float lemmas)
+    cudaError_t (*filter_f32)(const LevelArgs& a, cudaStream_t s);
+    cudaError_t (*level_esc)(int mode, const LevelArgs& a, unsigned blocks, cudaStream_t s);
 };
 
 template<class L, class T> cudaError_t launch_level(int mode, const LevelArgs& a, cudaStream_t s) {
@@ -342,6 +405,26 @@ template<class L, class T> cudaError_t launch_level(int mode, const LevelArgs& a
         case MODE_HULL: k_level<L, T, MODE_HULL><<<unsigned(blocks), threads, 0, s>>>(a); break;
         case MODE_CRIT: k_level<L, T, MODE_CRIT><<<unsigned(blocks), threads, 0, s>>>(a); break;
         case MODE_QUEUE: k_level<L, T, MODE_QUEUE><<<unsigned(blocks), threads, 0, s>>>(a); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template<class L> cudaError_t launch_filter_f32(const LevelArgs& a, cudaStream_t s) {
+    if(a.n_child == 0) return cudaSuccess;
+    const std::uint64_t blocks = (a.n_child + 127) / 128;
+    if(blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    k_filter_f32<L><<<unsigned(blocks), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template<class L> cudaError_t launch_level_esc(int mode, const LevelArgs& a, unsigned blocks, cudaStream_t s) {
+    if(blocks == 0) return cudaSuccess;
+    switch(mode) {
+        case MODE_EMIT: k_level_esc<L, MODE_EMIT><<<blocks, 128, 0, s>>>(a); break;
+        case MODE_HULL: k_level_esc<L, MODE_HULL><<<blocks, 128, 0, s>>>(a); break;
+        case MODE_CRIT: k_level_esc<L, MODE_CRIT><<<blocks, 128, 0, s>>>(a); break;
+        case MODE_QUEUE: k_level_esc<L, MODE_QUEUE><<<blocks, 128, 0, s>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
