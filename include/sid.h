@@ -146,6 +146,62 @@ int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, co
 int sid_leaf_hull_noalloc(sid_engine* engine, int lemma_id, const double* boxes, uint64_t n, double* hulls,
                           uint8_t* nonempty, unsigned long long* leaves, void* stream);
 
+/* ---- Served form: a request loop with continuous batching. No counterpart in the reference (its
+ * driver proves one lemma per run_prover call); an addition of this library for proving many lemmas
+ * and sub-boxes at once on one GPU.
+ *
+ * A server owns one worker thread and CUDA stream per lemma ("lane"). sid_submit queues a request: a
+ * whole lemma proof (boxes == NULL: the lemma's root box with its root partition, exactly as sid_prove)
+ * or a set of sub-boxes of the lemma (each enters the request's frontier as a depth-0 element and counts
+ * as one cuboid). Requests are admitted in arrival order while their frontier queues fit the memory
+ * budget; each admitted request keeps its frontier and counters on the device. Every step of a lane
+ * takes elements from all of its admitted requests at once (an equal share each, leftovers oldest
+ * first), so requests that arrive while others are running join the work already on the GPU; lanes of
+ * different lemmas run concurrently. The counts of a request do not depend on what else is running.
+ * The server must be destroyed before its engine; register lemmas before submitting requests for them. */
+typedef struct sid_server sid_server;
+
+typedef struct sid_server_opts {
+    uint64_t memory_budget_bytes;       /* device memory for request frontiers; 0: 16 GiB */
+    int64_t step_elements;              /* queue elements per lane step; <= 0: 65536 */
+    int32_t precision;                  /* SID_PRECISION_* for every request */
+    uint32_t generation_count;          /* generations per request; 0: 8 */
+    uint64_t max_criticals_per_request; /* critical boxes stored per request */
+    uint32_t max_requests_per_lane;     /* admitted at once per lemma; 0: 1024 */
+} sid_server_opts;
+
+#define SID_REQ_PENDING 0                /* waiting for admission */
+#define SID_REQ_RUNNING 1
+#define SID_REQ_DONE 2
+#define SID_REQ_FAILED 3                 /* see sid_last_error() after sid_request_poll/wait */
+
+typedef struct sid_request_status {
+    int32_t state;                      /* SID_REQ_* */
+    int32_t proved;                     /* DONE and no critical cuboid */
+    uint64_t num_cuboids;
+    uint64_t num_leaf_cuboids;
+    uint64_t num_critical_cuboids;
+    uint64_t escalated;                 /* children evaluated in FP64 (precision form) */
+    uint64_t criticals_stored;
+    double seconds_queued;              /* submission to admission */
+    double seconds_to_verdict;          /* submission to completion (host clock) */
+} sid_request_status;
+
+void sid_server_opts_default(sid_server_opts* opts);
+int sid_server_create(sid_engine* engine, const sid_server_opts* opts, sid_server** out);
+/* Stops the workers after the steps in flight; unfinished requests are dropped. */
+void sid_server_destroy(sid_server* server);
+/* boxes: NULL for the whole lemma, else nboxes * nargs (lo, hi) pairs, box-major: box b, variable v at
+ * boxes[2*(b*nargs + v)]. */
+int sid_submit(sid_server* server, int lemma_id, const double* boxes, uint64_t nboxes, uint64_t* request_id);
+int sid_request_poll(sid_server* server, uint64_t request_id, sid_request_status* status);
+/* Wait up to timeout_ms (< 0: no limit) for the request to finish; SID_ERR_TIMEOUT if it has not. */
+int sid_request_wait(sid_server* server, uint64_t request_id, int timeout_ms, sid_request_status* status);
+/* Critical boxes stored for a finished request, as sid_fetch_criticals. */
+int sid_request_criticals(sid_server* server, uint64_t request_id, double* out, uint64_t capacity, uint64_t* n_out);
+/* Forget a finished request. */
+int sid_request_release(sid_server* server, uint64_t request_id);
+
 #ifdef __cplusplus
 }
 #endif

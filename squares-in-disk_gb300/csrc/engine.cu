@@ -3,22 +3,34 @@
 // A proof replaces the reference's ProofDriver + prover core
 // (prover/proof_driver.hpp:218-627, cpu_prover/cpu_prover_core.hpp:31-260):
 //   init   root partition over the dynamic variables (proof_driver.hpp:320-391)
-//   loop   take a batch of queue elements (the queue is a device-resident LIFO stack);
+//   loop   take elements from the top of the queue (a device-resident LIFO stack);
 //          run the static-split levels with hull join (cpu_prover_core.hpp:221-256);
 //          route each hull: final generation -> static levels again, storing criticals
 //          (proof_driver.hpp:413-423); otherwise dynamic re-split into the queue with
 //          depth+1 (pd_impl_split_into.hpp:37-75).
 // Each level is one kernel launch over all (item, child) pairs; level lists are processed
-// in chunks so memory stays bounded. Cuboid counts are known on the host from the launch
-// sizes; leaf and critical counts are accumulated on the device.
+// in chunks so memory stays bounded. Counts are accumulated on the device per request.
+//
+// Work is organised in lanes: a lane owns the scratch of one lemma and serves any number of requests
+// of that lemma; every element carries the tag (slot) of its request, whose counters, frontier queue
+// and critical store live in a device table. sid_prove runs one request on a lane cached in the
+// engine; the server (sid_server_*) runs one lane per lemma on its own thread and stream and batches
+// the elements of all admitted requests of that lemma into each step.
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -27,6 +39,7 @@
 #include "engine.cuh"
 #include "engine_internal.hpp"
 #include "lemma_ir.hpp"
+#include "serve_plan.hpp"
 
 namespace sid {
 extern const LemmaKernels* const kAllLemmas[];
@@ -76,24 +89,43 @@ template<class F> int guarded(F&& f) {
     }
 }
 
-/// Owning device allocation.
+/// Owning device allocation; reserve_on allocates stream-ordered (freed in order on the same stream,
+/// without the device-wide synchronisation of cudaFree).
 template<class T> struct DevBuf {
     T* p = nullptr;
     std::size_t n = 0;
+    cudaStream_t ordered = nullptr;
     DevBuf() = default;
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
     ~DevBuf() { release(); }
     void release() {
-        if(p) cudaFree(p);
+        if(p) {
+            if(ordered) cudaFreeAsync(p, ordered);
+            else cudaFree(p);
+        }
         p = nullptr;
         n = 0;
+        ordered = nullptr;
     }
     void reserve(std::size_t count) {
         if(count <= n) return;
         release();
         cuda_check(cudaMalloc(&p, std::max<std::size_t>(count, 1) * sizeof(T)), "cudaMalloc");
         n = count;
+    }
+    void reserve_on(std::size_t count, cudaStream_t s) {
+        if(count <= n) return;
+        release();
+        cuda_check(cudaMallocAsync(reinterpret_cast<void**>(&p), std::max<std::size_t>(count, 1) * sizeof(T), s),
+                   "cudaMallocAsync");
+        n = count;
+        ordered = s;
+    }
+    void swap(DevBuf& o) {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+        std::swap(ordered, o.ordered);
     }
 };
 
@@ -105,8 +137,9 @@ struct BoxList {
     DevBuf<std::uint32_t> elem;
     DevBuf<std::uint64_t> path;
     DevBuf<std::uint8_t> depth;
+    DevBuf<std::uint32_t> tag;
 
-    void reserve(int na, std::uint64_t c, bool with_elem, bool with_path, bool with_depth) {
+    void reserve(int na, std::uint64_t c, bool with_elem, bool with_path, bool with_depth, bool with_tag) {
         if(c <= cap && na == nargs) return;
         nargs = na;
         cap = c;
@@ -115,6 +148,7 @@ struct BoxList {
         if(with_elem) { elem.release(); elem.reserve(c); }
         if(with_path) { path.release(); path.reserve(c); }
         if(with_depth) { depth.release(); depth.reserve(c); }
+        if(with_tag) { tag.release(); tag.reserve(c); }
     }
 };
 
@@ -122,30 +156,47 @@ struct Lemma {
     sid::LemmaIR ir;
     const sid::LemmaKernels* k = nullptr;
     DevBuf<double2> root;                // initial runtime box, computed once at registration
-    std::vector<double> criticals;       // from the last proof
+    std::vector<double> criticals;       // from the last sid_prove
+};
+
+using Clock = std::chrono::steady_clock;
+
+/// One request: a whole-lemma proof or a set of sub-boxes, with its device frontier and results.
+/// The lane thread owns the device parts; `view`, `state` and the times are shared under the server lock.
+struct Request {
+    std::uint64_t id = 0;
+    int lemma_id = -1;
+    Lemma* lem = nullptr;
+    int slot = -1;
+    bool full = true;                    // whole lemma (root partition) or sub-boxes
+    std::vector<double> boxes;           // sub-boxes, box-major (lo, hi) pairs
+    std::uint64_t nboxes = 0;
+    unsigned generations = 8;
+    std::uint64_t crit_cap = 0;
+    DevBuf<double2> qbox;
+    DevBuf<std::uint8_t> qdepth;
+    std::uint64_t qcap = 0;
+    DevBuf<double> crit;
+    std::uint64_t bytes = 0;             // device bytes held (frontier + critical store)
+    sid::ReqDev view{};                  // device counters after the last step
+    int state = SID_REQ_PENDING;
+    bool admitted = false;
+    std::string error;
+    Clock::time_point t_submit, t_admit, t_done;
+    std::vector<double> criticals;
 };
 
 } // namespace
 
-struct sid_engine {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::vector<std::unique_ptr<Lemma>> lemmas;
-    // scratch reused across proofs
-    int sm_count = 0;
-    DevBuf<unsigned long long> counters;   // [0] leaves [1] criticals [2] out_count [3] fin [4] nf
-                                           // [5] escalation list length [6] escalated in total
-    DevBuf<unsigned int> overflow;
-    DevBuf<std::uint32_t> esc;             // precision form: escalation list of one chunk of children
-    DevBuf<unsigned long long> hull;       // 4 * batch * nargs
-    DevBuf<double> crit;
-    BoxList queue, fin, nonfin;
-    std::vector<std::unique_ptr<BoxList>> stat_levels, dyn_levels;
-    DevBuf<double> batch_in_lo, batch_in_hi, batch_out_lo, batch_out_hi;
-    DevBuf<std::int8_t> batch_verdict;
-};
+struct sid_engine;
 
 namespace sid {
+
+constexpr std::uint64_t kLevelCapItems = std::uint64_t(8) << 20;   // items per intermediate level list
+constexpr std::uint64_t kDefaultStep = std::uint64_t(1) << 16;     // queue elements per step
+constexpr std::uint64_t kEscChunk = std::uint64_t(1) << 24;        // children per precision-form pass pair
+constexpr unsigned kEscBlocksPerSM = 8;                            // grid of the escalated (double) pass
+constexpr int kDefaultSlots = 1024;
 
 struct HullArgs {
     const unsigned long long* hull_lo;
@@ -153,13 +204,13 @@ struct HullArgs {
     const unsigned long long* hull_zlo;
     const unsigned long long* hull_zhi;
     const std::uint8_t* depth;          // depth of each batch element
-    std::uint64_t depth_stride_base;    // element e has depth depth[e + base]
+    const std::uint32_t* tag;           // request of each batch element
+    const ReqDev* req;
     std::uint32_t n_elem;
     int nargs;
-    unsigned generations;
-    // outputs: final (depth >= generations) and non-final hulls
-    double2* fin_box; std::uint8_t* fin_depth; unsigned long long* fin_count;
-    double2* nf_box; std::uint8_t* nf_depth; unsigned long long* nf_count;
+    // outputs: final (depth >= the request's generations) and non-final hulls
+    double2* fin_box; std::uint8_t* fin_depth; std::uint32_t* fin_tag; unsigned long long* fin_count;
+    double2* nf_box; std::uint8_t* nf_depth; std::uint32_t* nf_tag; unsigned long long* nf_count;
     std::uint64_t out_stride;
 };
 
@@ -170,11 +221,13 @@ __global__ void k_hull_finalize(const HullArgs h) {
     if(e >= h.n_elem) return;
     const std::uint64_t b0 = std::uint64_t(e) * h.nargs;
     if(h.hull_lo[b0] == ~0ull) return;           // no leaf survived
-    const std::uint8_t d = h.depth[h.depth_stride_base + e];
-    const bool fin = d >= h.generations;
+    const std::uint8_t d = h.depth[e];
+    const std::uint32_t t = h.tag[e];
+    const bool fin = d >= h.req[t].generations;
     unsigned long long slot = atomicAdd(fin ? h.fin_count : h.nf_count, 1ull);
     double2* out = fin ? h.fin_box : h.nf_box;
     (fin ? h.fin_depth : h.nf_depth)[slot] = d;
+    (fin ? h.fin_tag : h.nf_tag)[slot] = t;
     for(int v = 0; v < h.nargs; ++v) {
         double lo = key_value(h.hull_lo[b0 + v]);
         double hi = key_value(h.hull_hi[b0 + v]);
@@ -185,157 +238,304 @@ __global__ void k_hull_finalize(const HullArgs h) {
 }
 
 /// Lemmas without static splits: every element is itself the only leaf of its static recursion
-/// (cpu_prover_core.hpp:250-256). Route elements [base, base+n) by depth like k_hull_finalize.
-__global__ void k_route_elements(const double2* box, std::uint64_t stride, const std::uint8_t* depth, std::uint64_t base,
-                                 std::uint64_t n, int nargs, unsigned generations,
-                                 double2* fin_box, std::uint8_t* fin_depth, unsigned long long* fin_count,
-                                 double2* nf_box, std::uint8_t* nf_depth, unsigned long long* nf_count,
-                                 std::uint64_t out_stride) {
+/// (cpu_prover_core.hpp:250-256). Count it and route it by depth like k_hull_finalize.
+__global__ void k_route_elements(const double2* box, std::uint64_t stride, const std::uint8_t* depth,
+                                 const std::uint32_t* tag, std::uint64_t n, int nargs, ReqDev* req,
+                                 double2* fin_box, std::uint8_t* fin_depth, std::uint32_t* fin_tag,
+                                 unsigned long long* fin_count, double2* nf_box, std::uint8_t* nf_depth,
+                                 std::uint32_t* nf_tag, unsigned long long* nf_count, std::uint64_t out_stride) {
     const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if(i >= n) return;
-    const std::uint8_t d = depth[base + i];
-    const bool fin = d >= generations;
+    const std::uint8_t d = depth[i];
+    const std::uint32_t t = tag[i];
+    atomicAdd(&req[t].cnt[RC_LEAVES], 1ull);
+    const bool fin = d >= req[t].generations;
     const unsigned long long slot = atomicAdd(fin ? fin_count : nf_count, 1ull);
     double2* out = fin ? fin_box : nf_box;
     (fin ? fin_depth : nf_depth)[slot] = d;
-    for(int v = 0; v < nargs; ++v) out[std::uint64_t(v) * out_stride + slot] = box[std::uint64_t(v) * stride + base + i];
+    (fin ? fin_tag : nf_tag)[slot] = t;
+    for(int v = 0; v < nargs; ++v) out[std::uint64_t(v) * out_stride + slot] = box[std::uint64_t(v) * stride + i];
 }
 
-/// Lemmas without static splits, final generation: every element is a critical.
-__global__ void k_store_criticals(const double2* box, std::uint64_t stride, std::uint64_t n, int nargs, double* crit,
-                                  std::uint64_t crit_cap, unsigned long long* crit_count) {
+/// Lemmas without static splits, final generation: every element is a leaf and a critical.
+__global__ void k_store_criticals(const double2* box, std::uint64_t stride, const std::uint32_t* tag, std::uint64_t n,
+                                  int nargs, ReqDev* req) {
     const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if(i >= n) return;
-    const unsigned long long slot = atomicAdd(crit_count, 1ull);
-    if(slot >= crit_cap) return;
+    ReqDev* r = req + tag[i];
+    atomicAdd(&r->cnt[RC_LEAVES], 1ull);
+    const unsigned long long slot = atomicAdd(&r->cnt[RC_CRITICALS], 1ull);
+    if(slot >= r->crit_cap) return;
     for(int v = 0; v < nargs; ++v) {
         double2 b = box[std::uint64_t(v) * stride + i];
-        crit[(slot * nargs + v) * 2] = b.x;
-        crit[(slot * nargs + v) * 2 + 1] = b.y;
+        r->crit[(slot * nargs + v) * 2] = b.x;
+        r->crit[(slot * nargs + v) * 2 + 1] = b.y;
     }
 }
 
-} // namespace sid
+struct GatherEntry {
+    std::uint32_t slot;
+    std::uint32_t pad;
+    unsigned long long begin, count, dst;
+};
 
-namespace {
+/// Copy the elements [begin, begin + count) of each entry's request queue to the step batch at dst, and
+/// pop them (the request's queue size becomes begin; its children are appended from there).
+__global__ void k_gather(const GatherEntry* ent, int n_ent, unsigned long long total, ReqDev* req, int nargs,
+                         double2* dst_box, std::uint64_t dst_stride, std::uint8_t* dst_depth, std::uint32_t* dst_tag) {
+    const unsigned long long i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(i >= total) return;
+    int lo = 0, hi = n_ent - 1;                  // last entry with dst <= i
+    while(lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if(ent[mid].dst <= i) lo = mid; else hi = mid - 1;
+    }
+    const GatherEntry g = ent[lo];
+    const ReqDev* r = req + g.slot;
+    const unsigned long long src = g.begin + (i - g.dst);
+    for(int v = 0; v < nargs; ++v) dst_box[std::uint64_t(v) * dst_stride + i] = r->qbox[std::uint64_t(v) * r->qcap + src];
+    dst_depth[i] = r->qdepth[src];
+    dst_tag[i] = g.slot;
+    if(i == g.dst) req[g.slot].cnt[RC_QSIZE] = g.begin;
+}
 
-using namespace sid;
-
-constexpr std::uint64_t kLevelCapItems = std::uint64_t(8) << 20;   // items per intermediate level list
-constexpr std::uint64_t kDefaultBatch = std::uint64_t(1) << 16;    // queue elements per step
-constexpr std::uint64_t kEscChunk = std::uint64_t(1) << 24;        // children per precision-form pass pair
-constexpr unsigned kEscBlocksPerSM = 8;                            // grid of the escalated (double) pass
-
-struct Prover {
-    sid_engine* eng;
-    Lemma* lem;
-    const sid_prove_opts& opts;
+/// Lane: the scratch of one lemma and the device table of the requests it serves. Not thread-safe:
+/// one host thread drives a lane.
+struct Lane {
+    sid_engine* eng = nullptr;
+    Lemma* lem = nullptr;
     int n = 0;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
     std::vector<IrSplit> dyn, stat;
-    std::uint64_t batch = kDefaultBatch;
-    std::uint64_t qsize = 0;
-    std::uint64_t cuboids = 0;
-    unsigned long long* d_leaf = nullptr;
-    unsigned long long* d_crit = nullptr;
-    unsigned long long* d_out = nullptr;
-    unsigned long long* d_fin = nullptr;
-    unsigned long long* d_nf = nullptr;
-    std::uint64_t crit_cap = 0;
-    std::uint64_t host_leaves = 0;     // leaves counted on the host (lemmas without static splits)
-    bool fp32_first = false;           // precision form
-    unsigned long long* d_esc = nullptr;
-    unsigned long long* d_esc_total = nullptr;
+    std::uint64_t step_cap = kDefaultStep;
+    bool fp32_first = false;
+    std::uint64_t fanout = 1, root_fanout = 1;
+    int sm_count = 1;
+    int max_slots = kDefaultSlots;
+    DevBuf<ReqDev> req_dev;
+    std::vector<ReqDev> req_host;          // host copy of the table (counters as of the last read)
+    std::vector<Request*> slot_req;
+    DevBuf<unsigned long long> counters;   // [0] out_count [1] fin [2] nf [3] escalation list length
+    DevBuf<unsigned int> overflow;
+    DevBuf<unsigned long long> hull;       // 4 * step_cap * nargs
+    BoxList step, fin, nonfin;
+    std::vector<std::unique_ptr<BoxList>> stat_levels, dyn_levels;
+    DevBuf<std::uint32_t> esc;
+    DevBuf<GatherEntry> gather;
+    std::vector<GatherEntry> gather_host;
+    long long grown_bytes = 0;             // device bytes request queues grew by since the last take_grown_bytes
 
-    Prover(sid_engine* e, Lemma* l, const sid_prove_opts& o) : eng(e), lem(l), opts(o) {
+    Lane(sid_engine* e, Lemma* l, cudaStream_t s, bool own, int sms, int slots)
+        : eng(e), lem(l), st(s), own_stream(own), sm_count(sms), max_slots(slots) {
         n = l->ir.nargs;
         dyn = l->ir.dynamic_splits();
         stat = l->ir.static_splits();
-        if(o.batch_elements > 0) batch = std::uint64_t(o.batch_elements);
-        fp32_first = o.precision == SID_PRECISION_FP32_ESCALATE && l->k->filter_f32 != nullptr;
+        for(const auto& sp : dyn) {
+            fanout *= std::uint64_t(sp.subdivisions);
+            root_fanout *= std::uint64_t(sp.initial);
+        }
+        req_host.assign(std::size_t(max_slots), ReqDev{});
+        slot_req.assign(std::size_t(max_slots), nullptr);
+        req_dev.reserve(std::size_t(max_slots));
+        cuda_check(cudaMemsetAsync(req_dev.p, 0, sizeof(ReqDev) * std::size_t(max_slots), st), "request table");
+        counters.reserve(8);
+        overflow.reserve(1);
+        cuda_check(cudaMemsetAsync(overflow.p, 0, sizeof(unsigned int), st), "overflow flag");
+    }
+    Lane(const Lane&) = delete;
+    Lane& operator=(const Lane&) = delete;
+    ~Lane() {
+        if(st) cudaStreamSynchronize(st);
+        if(own_stream && st) cudaStreamDestroy(st);
     }
 
-    cudaStream_t s() const { return eng->stream; }
+    void configure(std::uint64_t step_elements, bool fp32) {
+        step_cap = step_elements > 0 ? step_elements : kDefaultStep;
+        fp32_first = fp32 && lem->k->filter_f32 != nullptr;
+        hull.reserve(4 * step_cap * std::uint64_t(n));
+        step.reserve(n, std::max(step.cap, step_cap), false, false, true, true);
+        fin.reserve(n, std::max(fin.cap, step_cap), false, false, true, true);
+        nonfin.reserve(n, std::max(nonfin.cap, step_cap), false, false, true, true);
+        if(fp32_first) esc.reserve(kEscChunk);
+    }
+
+    long long take_grown_bytes() {
+        long long d = grown_bytes;
+        grown_bytes = 0;
+        return d;
+    }
+
+    const ReqDev& counters_of(const Request* r) const { return req_host[std::size_t(r->slot)]; }
+    std::uint64_t queue_size(const Request* r) const { return counters_of(r).cnt[RC_QSIZE]; }
 
     unsigned long long read_counter(unsigned long long* d) {
         unsigned long long v = 0;
-        cuda_check(cudaMemcpyAsync(&v, d, sizeof(v), cudaMemcpyDeviceToHost, s()), "read counter");
-        cuda_check(cudaStreamSynchronize(s()), "stream sync");
+        cuda_check(cudaMemcpyAsync(&v, d, sizeof(v), cudaMemcpyDeviceToHost, st), "read counter");
+        cuda_check(cudaStreamSynchronize(st), "stream sync");
         return v;
     }
     void set_counter(unsigned long long* d, unsigned long long v) {
-        cuda_check(cudaMemcpyAsync(d, &v, sizeof(v), cudaMemcpyHostToDevice, s()), "set counter");
+        cuda_check(cudaMemcpyAsync(d, &v, sizeof(v), cudaMemcpyHostToDevice, st), "set counter");
+    }
+
+    int free_slots() const {
+        int k = 0;
+        for(auto* r : slot_req) k += r ? 0 : 1;
+        return k;
+    }
+
+    std::uint64_t initial_queue_cap(const Request& r) const {
+        return std::max<std::uint64_t>(r.full ? root_fanout : r.nboxes, 64);
+    }
+    /// Device bytes a request holds right after admission.
+    std::uint64_t initial_bytes(const Request& r) const {
+        return plan::request_bytes(n, initial_queue_cap(r), std::max<std::uint64_t>(r.crit_cap, 1));
+    }
+
+    /// Write the queue pointers and capacity of a slot without touching its device counters.
+    void patch_queue(int slot) {
+        const ReqDev& h = req_host[std::size_t(slot)];
+        char* dst = reinterpret_cast<char*>(req_dev.p + slot) + offsetof(ReqDev, qbox);
+        const char* src = reinterpret_cast<const char*>(&h) + offsetof(ReqDev, qbox);
+        cuda_check(cudaMemcpyAsync(dst, src, offsetof(ReqDev, crit) - offsetof(ReqDev, qbox), cudaMemcpyHostToDevice, st),
+                   "request queue patch");
+        cuda_check(cudaStreamSynchronize(st), "request queue patch");
+    }
+
+    /// Admit a request: device slot, frontier queue, critical store; then its root partition (whole
+    /// lemma) or its sub-boxes as depth-0 elements.
+    void admit(Request* r) {
+        int slot = -1;
+        for(int i = 0; i < max_slots; ++i) {
+            if(!slot_req[std::size_t(i)]) { slot = i; break; }
+        }
+        if(slot < 0) fail(SID_ERR_CAPACITY, "no free request slot");
+        r->slot = slot;
+        slot_req[std::size_t(slot)] = r;
+        r->qcap = initial_queue_cap(*r);
+        r->qbox.reserve_on(std::size_t(n) * r->qcap, st);
+        r->qdepth.reserve_on(r->qcap, st);
+        r->crit.reserve_on(std::max<std::uint64_t>(r->crit_cap, 1) * 2 * std::uint64_t(n), st);
+        r->bytes = initial_bytes(*r);
+        ReqDev& h = req_host[std::size_t(slot)];
+        h = ReqDev{};
+        h.qbox = r->qbox.p;
+        h.qdepth = r->qdepth.p;
+        h.qcap = r->qcap;
+        h.crit = r->crit.p;
+        h.crit_cap = r->crit_cap;
+        h.generations = r->generations;
+        if(!r->full) {
+            h.cnt[RC_QSIZE] = r->nboxes;
+            h.cnt[RC_CUBOIDS] = r->nboxes;
+            std::vector<double2> col(std::size_t(r->nboxes));
+            for(int v = 0; v < n; ++v) {
+                for(std::uint64_t b = 0; b < r->nboxes; ++b) {
+                    const std::size_t k = std::size_t(2 * (b * std::uint64_t(n) + std::uint64_t(v)));
+                    col[std::size_t(b)] = make_double2(r->boxes[k], r->boxes[k + 1]);
+                }
+                cuda_check(cudaMemcpyAsync(r->qbox.p + std::uint64_t(v) * r->qcap, col.data(),
+                                           col.size() * sizeof(double2), cudaMemcpyHostToDevice, st), "sub-box upload");
+                cuda_check(cudaStreamSynchronize(st), "sub-box upload");
+            }
+            cuda_check(cudaMemsetAsync(r->qdepth.p, 0, std::size_t(r->nboxes), st), "sub-box depth");
+        }
+        cuda_check(cudaMemcpyAsync(req_dev.p + slot, &h, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
+        cuda_check(cudaStreamSynchronize(st), "request slot");
+        if(r->full) run_dynamic(0, lem->root.p, 1, nullptr, nullptr, std::uint32_t(slot), 0, 1, true, 0);
+        read_slots();
+    }
+
+    /// Drop a request's device state (after completion or failure).
+    void release(Request* r) {
+        if(r->slot < 0) return;
+        cuda_check(cudaStreamSynchronize(st), "release sync");
+        slot_req[std::size_t(r->slot)] = nullptr;
+        req_host[std::size_t(r->slot)] = ReqDev{};
+        r->slot = -1;
+        r->qbox.release();
+        r->qdepth.release();
+        r->crit.release();
+    }
+
+    /// Copy the counters of the used slots from the device table; checks the overflow flags.
+    void read_slots() {
+        int hi = 0;
+        for(int i = 0; i < max_slots; ++i) if(slot_req[std::size_t(i)]) hi = i + 1;
+        std::vector<ReqDev> tmp(std::size_t(std::max(hi, 1)));
+        unsigned int ovf = 0;
+        if(hi > 0) {
+            cuda_check(cudaMemcpyAsync(tmp.data(), req_dev.p, sizeof(ReqDev) * std::size_t(hi), cudaMemcpyDeviceToHost, st),
+                       "request table");
+        }
+        cuda_check(cudaMemcpyAsync(&ovf, overflow.p, sizeof(ovf), cudaMemcpyDeviceToHost, st), "overflow flag");
+        cuda_check(cudaStreamSynchronize(st), "request table sync");
+        if(ovf) fail(SID_ERR_CUDA, "internal error: a level list overflowed");
+        for(int i = 0; i < hi; ++i) {
+            if(!slot_req[std::size_t(i)]) continue;
+            std::memcpy(req_host[std::size_t(i)].cnt, tmp[std::size_t(i)].cnt, sizeof(tmp[0].cnt));
+            if(tmp[std::size_t(i)].cnt[RC_OVERFLOW]) fail(SID_ERR_CUDA, "internal error: a request queue overflowed");
+        }
+    }
+
+    /// Critical boxes stored for a request (after it finished).
+    void fetch_criticals(Request* r) {
+        const std::uint64_t k = std::min<std::uint64_t>(counters_of(r).cnt[RC_CRITICALS], r->crit_cap);
+        r->criticals.assign(std::size_t(k * 2 * std::uint64_t(n)), 0.0);
+        if(k) {
+            cuda_check(cudaMemcpyAsync(r->criticals.data(), r->crit.p, r->criticals.size() * sizeof(double),
+                                       cudaMemcpyDeviceToHost, st), "copy criticals");
+            cuda_check(cudaStreamSynchronize(st), "copy criticals");
+        }
     }
 
     LevelArgs base_args() {
         LevelArgs a{};
-        a.leaf_count = d_leaf;
-        a.crit_count = d_crit;
-        a.crit = eng->crit.p;
-        a.crit_cap = crit_cap;
-        a.overflow = eng->overflow.p;
-        a.out_count = d_out;
+        a.req = req_dev.p;
+        a.overflow = overflow.p;
+        a.out_count = counters.p;
         return a;
     }
 
     void launch(int mode, const LevelArgs& a0) {
         const std::uint64_t total = a0.n_in * std::uint64_t(a0.nsub);
-        cuboids += total;
+        if(total == 0) return;
         if(!fp32_first) {
-            cuda_check(lem->k->level(mode, a0, s()), "level kernel launch");
+            LevelArgs a = a0;
+            a.count_cuboids = true;
+            cuda_check(lem->k->level(mode, a, st), "level kernel launch");
             return;
         }
         // precision form: float pass over a chunk of children, then double pass over its escalation list
         for(std::uint64_t cb = 0; cb < total; cb += kEscChunk) {
             LevelArgs a = a0;
+            a.count_cuboids = false;
             a.child_begin = cb;
             a.n_child = std::min(kEscChunk, total - cb);
-            a.esc = eng->esc.p;
-            a.esc_count = d_esc;
-            a.esc_total = d_esc_total;
-            cuda_check(cudaMemsetAsync(d_esc, 0, sizeof(unsigned long long), s()), "reset escalation count");
-            cuda_check(lem->k->filter_f32(a, s()), "float pass launch");
+            a.esc = esc.p;
+            a.esc_count = counters.p + 3;
+            cuda_check(cudaMemsetAsync(a.esc_count, 0, sizeof(unsigned long long), st), "reset escalation count");
+            cuda_check(lem->k->filter_f32(a, st), "float pass launch");
             const std::uint64_t want = (a.n_child + 127) / 128;
-            const unsigned blocks = unsigned(std::min<std::uint64_t>(want, std::uint64_t(eng->sm_count) * kEscBlocksPerSM));
-            cuda_check(lem->k->level_esc(mode, a, blocks, s()), "escalated pass launch");
+            const unsigned blocks = unsigned(std::min<std::uint64_t>(want, std::uint64_t(sm_count) * kEscBlocksPerSM));
+            cuda_check(lem->k->level_esc(mode, a, blocks, st), "escalated pass launch");
         }
     }
 
     BoxList& stat_level(std::size_t j) {
-        while(eng->stat_levels.size() <= j) eng->stat_levels.emplace_back(new BoxList);
-        return *eng->stat_levels[j];
+        while(stat_levels.size() <= j) stat_levels.emplace_back(new BoxList);
+        return *stat_levels[j];
     }
     BoxList& dyn_level(std::size_t j) {
-        while(eng->dyn_levels.size() <= j) eng->dyn_levels.emplace_back(new BoxList);
-        return *eng->dyn_levels[j];
+        while(dyn_levels.size() <= j) dyn_levels.emplace_back(new BoxList);
+        return *dyn_levels[j];
     }
 
-    /// Ensure the queue can hold `need` elements, preserving its first qsize entries.
-    void queue_reserve(std::uint64_t need) {
-        BoxList& q = eng->queue;
-        if(need <= q.cap && q.nargs == n) return;
-        std::uint64_t ncap = std::max<std::uint64_t>(need, q.nargs == n ? q.cap * 2 : 0);
-        ncap = std::max<std::uint64_t>(ncap, 1 << 16);
-        DevBuf<double2> nb;
-        DevBuf<std::uint8_t> nd;
-        nb.reserve(std::size_t(n) * ncap);
-        nd.reserve(ncap);
-        if(qsize > 0 && q.nargs == n) {
-            for(int v = 0; v < n; ++v) {
-                cuda_check(cudaMemcpyAsync(nb.p + std::uint64_t(v) * ncap, q.box.p + std::uint64_t(v) * q.cap,
-                                           qsize * sizeof(double2), cudaMemcpyDeviceToDevice, s()), "queue grow");
-            }
-            cuda_check(cudaMemcpyAsync(nd.p, q.depth.p, qsize, cudaMemcpyDeviceToDevice, s()), "queue grow");
-        }
-        cuda_check(cudaStreamSynchronize(s()), "queue grow sync");
-        std::swap(q.box.p, nb.p); std::swap(q.box.n, nb.n);
-        std::swap(q.depth.p, nd.p); std::swap(q.depth.n, nd.n);
-        q.cap = ncap;
-        q.nargs = n;
-    }
-
-    /// Dynamic levels d.. (root partition or re-split). Input items carry a depth.
+    /// Dynamic levels d.. (root partition or re-split); the last one appends to the requests' queues.
     void run_dynamic(std::size_t d, const double2* in_box, std::uint64_t in_stride, const std::uint8_t* in_depth,
-                     std::uint8_t depth_value, std::uint64_t n_in, bool initial, std::uint8_t depth_add) {
+                     const std::uint32_t* in_tag, std::uint32_t tag_value, std::uint8_t depth_value, std::uint64_t n_in,
+                     bool initial, std::uint8_t depth_add) {
         const IrSplit& sp = dyn[d];
         const int nsub = int(initial ? sp.initial : sp.subdivisions);
         const int it_limit = 2 * n;
@@ -348,7 +548,7 @@ struct Prover {
         } else {
             out = &dyn_level(d + 1);
             std::uint64_t cap = std::min<std::uint64_t>(kLevelCapItems, std::max<std::uint64_t>(n_in, 1) * nsub);
-            out->reserve(n, std::max(out->cap, cap), false, false, true);
+            out->reserve(n, std::max(out->cap, cap), false, false, true, true);
             chunk = std::max<std::uint64_t>(1, out->cap / std::uint64_t(nsub));
         }
         for(std::uint64_t off = 0; off < n_in; off += chunk) {
@@ -357,6 +557,8 @@ struct Prover {
             a.in_box = in_box;
             a.in_stride = in_stride;
             a.in_depth = in_depth;
+            a.in_tag = in_tag;
+            a.tag_value = tag_value;
             a.depth_value = depth_value;
             a.in_begin = off;
             a.n_in = len;
@@ -365,34 +567,29 @@ struct Prover {
             a.it_limit = it_limit;
             a.rec_limit = rec_limit;
             if(last) {
-                queue_reserve(qsize + len * std::uint64_t(nsub));
                 a.row_begin = n - 1;
                 a.row_end = n;
-                a.out_box = eng->queue.box.p;
-                a.out_stride = eng->queue.cap;
-                a.out_cap = eng->queue.cap;
-                a.out_depth = eng->queue.depth.p;
                 a.depth_add = depth_add;
-                set_counter(d_out, qsize);
                 launch(MODE_QUEUE, a);
-                qsize = read_counter(d_out);
             } else {
                 a.row_begin = a.row_end = 0;
                 a.out_box = out->box.p;
                 a.out_stride = out->cap;
                 a.out_cap = out->cap;
                 a.out_depth = out->depth.p;
-                set_counter(d_out, 0);
+                a.out_tag = out->tag.p;
+                set_counter(counters.p, 0);
                 launch(MODE_EMIT, a);
-                std::uint64_t cnt = read_counter(d_out);
-                run_dynamic(d + 1, out->box.p, out->cap, out->depth.p, 0, cnt, initial, depth_add);
+                std::uint64_t cnt = read_counter(counters.p);
+                run_dynamic(d + 1, out->box.p, out->cap, out->depth.p, out->tag.p, 0, 0, cnt, initial, depth_add);
             }
         }
     }
 
     /// Static levels j.. over items; innermost level joins hulls (MODE_HULL) or stores criticals (MODE_CRIT).
     void run_static(std::size_t j, const double2* in_box, std::uint64_t in_stride, const std::uint32_t* in_elem,
-                    const std::uint64_t* in_path, std::uint64_t in_begin, std::uint64_t n_in, int final_mode) {
+                    const std::uint64_t* in_path, const std::uint32_t* elem_tag, std::uint64_t in_begin, std::uint64_t n_in,
+                    int final_mode) {
         const IrSplit& sp = stat[j];
         const int nsub = int(sp.subdivisions);
         const bool last = j + 1 == stat.size();
@@ -402,182 +599,152 @@ struct Prover {
             for(std::uint64_t off = 0; off < n_in; off += chunk) {
                 LevelArgs a = base_args();
                 a.in_box = in_box; a.in_stride = in_stride; a.in_elem = in_elem; a.in_path = in_path;
+                a.elem_tag = elem_tag;
                 a.in_begin = in_begin + off; a.n_in = std::min(chunk, n_in - off);
                 a.elem_base = std::uint32_t(off);
                 a.var = sp.arg; a.nsub = nsub; a.it_limit = n; a.rec_limit = 4;
                 a.row_begin = sp.arg; a.row_end = row_end;
-                a.hull_lo = eng->hull.p;
-                a.hull_hi = eng->hull.p + batch * n;
-                a.hull_zlo = eng->hull.p + 2 * batch * n;
-                a.hull_zhi = eng->hull.p + 3 * batch * n;
+                a.hull_lo = hull.p;
+                a.hull_hi = hull.p + step_cap * n;
+                a.hull_zlo = hull.p + 2 * step_cap * n;
+                a.hull_zhi = hull.p + 3 * step_cap * n;
                 launch(final_mode, a);
             }
             return;
         }
         BoxList& out = stat_level(j + 1);
         std::uint64_t cap = std::min<std::uint64_t>(kLevelCapItems, std::max<std::uint64_t>(n_in, 1) * nsub);
-        out.reserve(n, std::max(out.cap, cap), true, true, false);
+        out.reserve(n, std::max(out.cap, cap), true, true, false, false);
         const std::uint64_t chunk = std::max<std::uint64_t>(1, out.cap / std::uint64_t(nsub));
         for(std::uint64_t off = 0; off < n_in; off += chunk) {
             LevelArgs a = base_args();
             a.in_box = in_box; a.in_stride = in_stride; a.in_elem = in_elem; a.in_path = in_path;
+            a.elem_tag = elem_tag;
             a.in_begin = in_begin + off; a.n_in = std::min(chunk, n_in - off);
             a.elem_base = std::uint32_t(off);
             a.var = sp.arg; a.nsub = nsub; a.it_limit = n; a.rec_limit = 4;
             a.row_begin = sp.arg; a.row_end = row_end;
             a.out_box = out.box.p; a.out_stride = out.cap; a.out_cap = out.cap;
             a.out_elem = out.elem.p; a.out_path = out.path.p;
-            set_counter(d_out, 0);
+            set_counter(counters.p, 0);
             launch(MODE_EMIT, a);
-            std::uint64_t cnt = read_counter(d_out);
-            run_static(j + 1, out.box.p, out.cap, out.elem.p, out.path.p, 0, cnt, final_mode);
+            std::uint64_t cnt = read_counter(counters.p);
+            run_static(j + 1, out.box.p, out.cap, out.elem.p, out.path.p, elem_tag, 0, cnt, final_mode);
         }
     }
 
-    void progress(std::chrono::steady_clock::time_point t0, std::chrono::steady_clock::time_point& last_cb, bool& first_done) {
-        if(!opts.progress) return;
-        auto now = std::chrono::steady_clock::now();
-        auto since_start = std::chrono::duration_cast<std::chrono::milliseconds>(now - t0).count();
-        auto since_last = std::chrono::duration_cast<std::chrono::milliseconds>(now - last_cb).count();
-        if(!first_done ? since_start < long(opts.progress_first_ms) : since_last < long(opts.progress_every_ms)) return;
-        first_done = true;
-        last_cb = now;
-        sid_progress p{};
-        p.queue_size = qsize;
-        p.cuboid_count = cuboids;
-        p.leaf_count = read_counter(d_leaf);
-        p.critical_count = read_counter(d_crit);
-        std::vector<double> head(std::size_t(2 * n));
-        if(qsize > 0) {
-            for(int v = 0; v < n; ++v) {
-                double2 b;
-                cuda_check(cudaMemcpy(&b, eng->queue.box.p + std::uint64_t(v) * eng->queue.cap + qsize - 1, sizeof(b),
-                                      cudaMemcpyDeviceToHost), "queue head");
-                head[std::size_t(2 * v)] = b.x;
-                head[std::size_t(2 * v + 1)] = b.y;
-            }
-            p.queue_head = head.data();
+    /// Make room in a request's queue before a step takes `taken` of its elements.
+    void ensure_queue(Request* r, std::uint64_t taken) {
+        const std::uint64_t qsize = queue_size(r);
+        const std::uint64_t need = plan::queue_need(qsize, taken, fanout);
+        if(need <= r->qcap) return;
+        const std::uint64_t ncap = plan::grow_capacity(r->qcap, need);
+        DevBuf<double2> nb;
+        DevBuf<std::uint8_t> nd;
+        nb.reserve_on(std::size_t(n) * ncap, st);
+        nd.reserve_on(ncap, st);
+        for(int v = 0; v < n; ++v) {
+            cuda_check(cudaMemcpyAsync(nb.p + std::uint64_t(v) * ncap, r->qbox.p + std::uint64_t(v) * r->qcap,
+                                       qsize * sizeof(double2), cudaMemcpyDeviceToDevice, st), "queue grow");
         }
-        opts.progress(opts.progress_user, &p);
+        cuda_check(cudaMemcpyAsync(nd.p, r->qdepth.p, qsize, cudaMemcpyDeviceToDevice, st), "queue grow");
+        cuda_check(cudaStreamSynchronize(st), "queue grow sync");
+        r->qbox.swap(nb);
+        r->qdepth.swap(nd);
+        const std::uint64_t old_bytes = r->bytes;
+        r->qcap = ncap;
+        r->bytes = plan::request_bytes(n, r->qcap, std::max<std::uint64_t>(r->crit_cap, 1));
+        grown_bytes += (long long)(r->bytes - old_bytes);
+        ReqDev& h = req_host[std::size_t(r->slot)];
+        h.qbox = r->qbox.p;
+        h.qdepth = r->qdepth.p;
+        h.qcap = r->qcap;
+        patch_queue(r->slot);
     }
 
-    void run(sid_result* res) {
-        if(opts.max_iterations_per_node > 1) {
-            fail(SID_ERR_UNSUPPORTED, "max_iterations_per_node > 1 (re-iteration of a node) is not supported; use 1");
+    /// One step over the given active requests (arrival order). Returns the number of elements expanded.
+    std::uint64_t run_step(const std::vector<Request*>& active) {
+        std::vector<std::pair<int, std::uint64_t>> q;
+        for(Request* r : active) q.emplace_back(r->slot, queue_size(r));
+        const std::vector<plan::Take> takes = plan::fill_step(q, step_cap);
+        if(takes.empty()) return 0;
+        gather_host.clear();
+        std::uint64_t B = 0;
+        for(const auto& t : takes) {
+            Request* r = slot_req[std::size_t(t.slot)];
+            ensure_queue(r, t.count);
+            gather_host.push_back(GatherEntry{std::uint32_t(t.slot), 0u, t.begin, t.count, t.dst});
+            B = t.dst + t.count;
         }
-        crit_cap = opts.max_criticals_kept;
-        eng->counters.reserve(8);
-        eng->overflow.reserve(1);
-        eng->hull.reserve(4 * batch * std::uint64_t(n));
-        eng->crit.reserve(std::max<std::uint64_t>(1, crit_cap) * 2 * std::uint64_t(n));
-        d_leaf = eng->counters.p;
-        d_crit = eng->counters.p + 1;
-        d_out = eng->counters.p + 2;
-        d_fin = eng->counters.p + 3;
-        d_nf = eng->counters.p + 4;
-        d_esc = eng->counters.p + 5;
-        d_esc_total = eng->counters.p + 6;
-        if(fp32_first) eng->esc.reserve(kEscChunk);
-        cuda_check(cudaMemsetAsync(eng->counters.p, 0, 8 * sizeof(unsigned long long), s()), "memset counters");
-        cuda_check(cudaMemsetAsync(eng->overflow.p, 0, sizeof(unsigned int), s()), "memset overflow");
-        eng->fin.reserve(n, batch, false, false, true);
-        eng->nonfin.reserve(n, batch, false, false, true);
-        qsize = 0;
-        cuboids = 0;
+        gather.reserve(gather_host.size());
+        cuda_check(cudaMemcpyAsync(gather.p, gather_host.data(), gather_host.size() * sizeof(GatherEntry),
+                                   cudaMemcpyHostToDevice, st), "gather table");
+        k_gather<<<unsigned((B + 127) / 128), 128, 0, st>>>(gather.p, int(gather_host.size()), B, req_dev.p, n, step.box.p,
+                                                            step.cap, step.depth.p, step.tag.p);
+        cuda_check(cudaGetLastError(), "gather");
 
-        cudaEvent_t ev0, ev1;
-        cuda_check(cudaEventCreate(&ev0), "event");
-        cuda_check(cudaEventCreate(&ev1), "event");
-        cuda_check(cudaEventRecord(ev0, s()), "event record");
-        auto t0 = std::chrono::steady_clock::now();
-        auto last_cb = t0;
-        bool first_done = false;
-
-        // root partition of the lemma's initial runtime box
-        queue_reserve(1 << 16);
-        run_dynamic(0, lem->root.p, 1, nullptr, 0, 1, true, 0);
-
-        while(qsize > 0) {
-            const std::uint64_t B = std::min(qsize, batch);
-            const std::uint64_t base = qsize - B;
-            set_counter(d_fin, 0);
-            set_counter(d_nf, 0);
-            if(stat.empty()) {
-                host_leaves += B;
-                k_route_elements<<<unsigned((B + 127) / 128), 128, 0, s()>>>(
-                    eng->queue.box.p, eng->queue.cap, eng->queue.depth.p, base, B, n, opts.generation_count,
-                    eng->fin.box.p, eng->fin.depth.p, d_fin, eng->nonfin.box.p, eng->nonfin.depth.p, d_nf, batch);
-                cuda_check(cudaGetLastError(), "route elements");
-            } else {
-                // reset hulls: lo keys to max, hi keys to 0, first-zero paths to max
-                cuda_check(cudaMemsetAsync(eng->hull.p, 0xff, B * n * sizeof(unsigned long long), s()), "hull reset");
-                cuda_check(cudaMemsetAsync(eng->hull.p + batch * n, 0, B * n * sizeof(unsigned long long), s()), "hull reset");
-                cuda_check(cudaMemsetAsync(eng->hull.p + 2 * batch * n, 0xff, 2 * batch * n * sizeof(unsigned long long), s()), "hull reset");
-                run_static(0, eng->queue.box.p, eng->queue.cap, nullptr, nullptr, base, B, MODE_HULL);
-                finalize_hulls(B, base);
-            }
-            const std::uint64_t nfin = read_counter(d_fin);
-            const std::uint64_t nnf = read_counter(d_nf);
-            qsize = base;
-            if(nfin > 0) {
-                if(stat.empty()) {
-                    host_leaves += nfin;
-                    k_store_criticals<<<unsigned((nfin + 127) / 128), 128, 0, s()>>>(
-                        eng->fin.box.p, batch, nfin, n, eng->crit.p, crit_cap, d_crit);
-                    cuda_check(cudaGetLastError(), "store criticals");
-                } else {
-                    run_static(0, eng->fin.box.p, batch, nullptr, nullptr, 0, nfin, MODE_CRIT);
-                }
-            }
-            if(nnf > 0) run_dynamic(0, eng->nonfin.box.p, batch, eng->nonfin.depth.p, 0, nnf, false, 1);
-            progress(t0, last_cb, first_done);
-        }
-        finish(ev0, ev1, res);
-    }
-
-    void finalize_hulls(std::uint64_t B, std::uint64_t base) {
+        set_counter(counters.p + 1, 0);
+        set_counter(counters.p + 2, 0);
+        if(stat.empty()) {
+            k_route_elements<<<unsigned((B + 127) / 128), 128, 0, st>>>(
+                step.box.p, step.cap, step.depth.p, step.tag.p, B, n, req_dev.p, fin.box.p, fin.depth.p, fin.tag.p,
+                counters.p + 1, nonfin.box.p, nonfin.depth.p, nonfin.tag.p, counters.p + 2, step_cap);
+            cuda_check(cudaGetLastError(), "route elements");
+        } else {
+            // reset hulls: lo keys to max, hi keys to 0, first-zero paths to max
+            cuda_check(cudaMemsetAsync(hull.p, 0xff, B * n * sizeof(unsigned long long), st), "hull reset");
+            cuda_check(cudaMemsetAsync(hull.p + step_cap * n, 0, B * n * sizeof(unsigned long long), st), "hull reset");
+            cuda_check(cudaMemsetAsync(hull.p + 2 * step_cap * n, 0xff, 2 * step_cap * n * sizeof(unsigned long long), st),
+                       "hull reset");
+            run_static(0, step.box.p, step.cap, nullptr, nullptr, step.tag.p, 0, B, MODE_HULL);
             HullArgs h{};
-            h.hull_lo = eng->hull.p;
-            h.hull_hi = eng->hull.p + batch * n;
-            h.hull_zlo = eng->hull.p + 2 * batch * n;
-            h.hull_zhi = eng->hull.p + 3 * batch * n;
-            h.depth = eng->queue.depth.p;
-            h.depth_stride_base = base;
+            h.hull_lo = hull.p;
+            h.hull_hi = hull.p + step_cap * n;
+            h.hull_zlo = hull.p + 2 * step_cap * n;
+            h.hull_zhi = hull.p + 3 * step_cap * n;
+            h.depth = step.depth.p;
+            h.tag = step.tag.p;
+            h.req = req_dev.p;
             h.n_elem = std::uint32_t(B);
             h.nargs = n;
-            h.generations = opts.generation_count;
-            h.fin_box = eng->fin.box.p; h.fin_depth = eng->fin.depth.p; h.fin_count = d_fin;
-            h.nf_box = eng->nonfin.box.p; h.nf_depth = eng->nonfin.depth.p; h.nf_count = d_nf;
-            h.out_stride = batch;
-            k_hull_finalize<<<unsigned((B + 127) / 128), 128, 0, s()>>>(h);
+            h.fin_box = fin.box.p; h.fin_depth = fin.depth.p; h.fin_tag = fin.tag.p; h.fin_count = counters.p + 1;
+            h.nf_box = nonfin.box.p; h.nf_depth = nonfin.depth.p; h.nf_tag = nonfin.tag.p; h.nf_count = counters.p + 2;
+            h.out_stride = step_cap;
+            k_hull_finalize<<<unsigned((B + 127) / 128), 128, 0, st>>>(h);
             cuda_check(cudaGetLastError(), "hull finalize");
-    }
-
-    void finish(cudaEvent_t ev0, cudaEvent_t ev1, sid_result* res) {
-        cuda_check(cudaEventRecord(ev1, s()), "event record");
-        cuda_check(cudaEventSynchronize(ev1), "event sync");
-        float ms = 0;
-        cuda_check(cudaEventElapsedTime(&ms, ev0, ev1), "elapsed");
-        cudaEventDestroy(ev0);
-        cudaEventDestroy(ev1);
-
-        unsigned int ovf = 0;
-        cuda_check(cudaMemcpy(&ovf, eng->overflow.p, sizeof(ovf), cudaMemcpyDeviceToHost), "overflow flag");
-        if(ovf) fail(SID_ERR_CUDA, "internal error: a level list overflowed");
-        res->num_cuboids = cuboids;
-        res->num_leaf_cuboids = read_counter(d_leaf) + host_leaves;
-        res->num_critical_cuboids = read_counter(d_crit);
-        res->num_repeated_nodes = 0;
-        res->criticals_stored = std::min<std::uint64_t>(res->num_critical_cuboids, crit_cap);
-        res->escalated = fp32_first ? read_counter(d_esc_total) : 0;
-        res->seconds = double(ms) / 1000.0;
-        lem->criticals.assign(std::size_t(res->criticals_stored) * 2 * std::size_t(n), 0.0);
-        if(res->criticals_stored) {
-            cuda_check(cudaMemcpy(lem->criticals.data(), eng->crit.p, lem->criticals.size() * sizeof(double),
-                                  cudaMemcpyDeviceToHost), "copy criticals");
         }
+        const std::uint64_t nfin = read_counter(counters.p + 1);
+        const std::uint64_t nnf = read_counter(counters.p + 2);
+        if(nfin > 0) {
+            if(stat.empty()) {
+                k_store_criticals<<<unsigned((nfin + 127) / 128), 128, 0, st>>>(fin.box.p, step_cap, fin.tag.p, nfin, n,
+                                                                                 req_dev.p);
+                cuda_check(cudaGetLastError(), "store criticals");
+            } else {
+                run_static(0, fin.box.p, step_cap, nullptr, nullptr, fin.tag.p, 0, nfin, MODE_CRIT);
+            }
+        }
+        if(nnf > 0) run_dynamic(0, nonfin.box.p, step_cap, nonfin.depth.p, nonfin.tag.p, 0, 0, nnf, false, 1);
+        read_slots();
+        return B;
     }
 };
+
+} // namespace sid
+
+struct sid_engine {
+    int device = 0;
+    int sm_count = 1;
+    cudaStream_t stream = nullptr;
+    std::vector<std::unique_ptr<Lemma>> lemmas;
+    std::map<int, std::unique_ptr<sid::Lane>> prove_lanes;   // lanes of sid_prove, one per lemma
+    DevBuf<double> batch_in_lo, batch_in_hi, batch_out_lo, batch_out_hi;
+    DevBuf<std::int8_t> batch_verdict;
+};
+
+namespace {
+
+using namespace sid;
 
 Lemma* get_lemma(sid_engine* e, int id) {
     if(!e) fail(SID_ERR_INVALID, "null engine");
@@ -587,7 +754,219 @@ Lemma* get_lemma(sid_engine* e, int id) {
 
 void set_device(sid_engine* e) { cuda_check(cudaSetDevice(e->device), "cudaSetDevice"); }
 
+void check_precision(int precision) {
+    if(precision != SID_PRECISION_PLAIN && precision != SID_PRECISION_FP32_ESCALATE) {
+        fail(SID_ERR_INVALID, "unknown precision mode %d", precision);
+    }
+}
+
+/// A whole proof of one lemma (sid_prove): one request on the engine's lane of that lemma.
+void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_result* res) {
+    Lemma* lem = get_lemma(eng, lemma_id);
+    if(o.max_iterations_per_node > 1) {
+        fail(SID_ERR_UNSUPPORTED, "max_iterations_per_node > 1 (re-iteration of a node) is not supported; use 1");
+    }
+    auto& slot = eng->prove_lanes[lemma_id];
+    if(!slot) slot.reset(new Lane(eng, lem, eng->stream, false, eng->sm_count, 1));
+    Lane& lane = *slot;
+    lane.configure(o.batch_elements > 0 ? std::uint64_t(o.batch_elements) : kDefaultStep,
+                   o.precision == SID_PRECISION_FP32_ESCALATE);
+
+    Request r;
+    r.lem = lem;
+    r.lemma_id = lemma_id;
+    r.full = true;
+    r.generations = o.generation_count;
+    r.crit_cap = o.max_criticals_kept;
+
+    cudaEvent_t ev0, ev1;
+    cuda_check(cudaEventCreate(&ev0), "event");
+    cuda_check(cudaEventCreate(&ev1), "event");
+    ReqDev last{};
+    try {
+        cuda_check(cudaEventRecord(ev0, lane.st), "event record");
+        const auto t0 = Clock::now();
+        auto last_cb = t0;
+        bool first_done = false;
+        lane.admit(&r);
+        const std::vector<Request*> active{&r};
+        while(lane.queue_size(&r) > 0) {
+            lane.run_step(active);
+            if(o.progress) {
+                const auto now = Clock::now();
+                const long long since_start = std::chrono::duration_cast<std::chrono::milliseconds>(now - t0).count();
+                const long long since_last = std::chrono::duration_cast<std::chrono::milliseconds>(now - last_cb).count();
+                if(first_done ? since_last >= (long long)o.progress_every_ms : since_start >= (long long)o.progress_first_ms) {
+                    first_done = true;
+                    last_cb = now;
+                    const ReqDev& c = lane.counters_of(&r);
+                    sid_progress p{};
+                    p.queue_size = c.cnt[RC_QSIZE];
+                    p.cuboid_count = c.cnt[RC_CUBOIDS];
+                    p.leaf_count = c.cnt[RC_LEAVES];
+                    p.critical_count = c.cnt[RC_CRITICALS];
+                    std::vector<double> head(std::size_t(2 * lane.n));
+                    if(p.queue_size > 0) {
+                        for(int v = 0; v < lane.n; ++v) {
+                            double2 b;
+                            cuda_check(cudaMemcpyAsync(&b, r.qbox.p + std::uint64_t(v) * r.qcap + p.queue_size - 1, sizeof(b),
+                                                       cudaMemcpyDeviceToHost, lane.st), "queue head");
+                            cuda_check(cudaStreamSynchronize(lane.st), "queue head");
+                            head[std::size_t(2 * v)] = b.x;
+                            head[std::size_t(2 * v + 1)] = b.y;
+                        }
+                        p.queue_head = head.data();
+                    }
+                    o.progress(o.progress_user, &p);
+                }
+            }
+        }
+        cuda_check(cudaEventRecord(ev1, lane.st), "event record");
+        cuda_check(cudaEventSynchronize(ev1), "event sync");
+        lane.fetch_criticals(&r);
+        last = lane.counters_of(&r);
+    } catch(...) {
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        lane.release(&r);
+        throw;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    lane.release(&r);
+    res->num_cuboids = last.cnt[RC_CUBOIDS];
+    res->num_leaf_cuboids = last.cnt[RC_LEAVES];
+    res->num_critical_cuboids = last.cnt[RC_CRITICALS];
+    res->num_repeated_nodes = 0;
+    res->criticals_stored = std::min<std::uint64_t>(res->num_critical_cuboids, r.crit_cap);
+    res->escalated = last.cnt[RC_ESCALATED];
+    res->seconds = double(ms) / 1000.0;
+    lem->criticals = std::move(r.criticals);
+}
+
 } // namespace
+
+/// The served form: one worker thread, stream and lane per lemma.
+struct sid_server {
+    struct Worker {
+        int lemma_id = -1;
+        std::unique_ptr<sid::Lane> lane;
+        std::thread th;
+        std::deque<Request*> pending;
+        std::vector<Request*> active;
+        std::condition_variable cv;
+    };
+
+    sid_engine* eng = nullptr;
+    sid_server_opts opts{};
+    std::mutex mu;
+    std::condition_variable cv_done;
+    std::unordered_map<std::uint64_t, std::unique_ptr<Request>> reqs;
+    std::map<int, std::unique_ptr<Worker>> workers;
+    std::uint64_t next_id = 1;
+    std::uint64_t mem_used = 0;          // device bytes held by admitted requests
+    bool stopping = false;
+
+    std::uint64_t budget() const { return opts.memory_budget_bytes ? opts.memory_budget_bytes : (std::uint64_t(16) << 30); }
+
+    void fail_all(Worker& w, const std::string& msg) {
+        std::lock_guard<std::mutex> lk(mu);
+        for(Request* r : w.active) { r->state = SID_REQ_FAILED; r->error = msg; r->t_done = Clock::now(); }
+        for(Request* r : w.pending) { r->state = SID_REQ_FAILED; r->error = msg; r->t_done = Clock::now(); }
+        w.active.clear();
+        w.pending.clear();
+        cv_done.notify_all();
+    }
+
+    void worker_loop(Worker* w) {
+        std::vector<Request*> held;   // admitted requests whose device state must be released on exit
+        try {
+            cuda_check(cudaSetDevice(eng->device), "cudaSetDevice");
+            cudaStream_t s = nullptr;
+            cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+            Lemma* lem = eng->lemmas[std::size_t(w->lemma_id)].get();
+            const int slots = int(opts.max_requests_per_lane > 0 ? opts.max_requests_per_lane : kDefaultSlots);
+            w->lane.reset(new Lane(eng, lem, s, true, eng->sm_count, slots));
+            w->lane->configure(opts.step_elements > 0 ? std::uint64_t(opts.step_elements) : kDefaultStep,
+                               opts.precision == SID_PRECISION_FP32_ESCALATE);
+            Lane& lane = *w->lane;
+            for(;;) {
+                std::vector<Request*> admit;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    w->cv.wait(lk, [&] { return stopping || !w->pending.empty() || !w->active.empty(); });
+                    if(stopping) break;
+                    std::vector<std::uint64_t> need;
+                    for(Request* r : w->pending) need.push_back(lane.initial_bytes(*r));
+                    const std::size_t k = plan::admit_count(need, mem_used, budget(), w->active.size(),
+                                                            std::size_t(lane.free_slots()));
+                    for(std::size_t i = 0; i < k; ++i) {
+                        admit.push_back(w->pending.front());
+                        w->pending.pop_front();
+                        mem_used += need[i];
+                    }
+                }
+                for(Request* r : admit) {
+                    held.push_back(r);
+                    lane.admit(r);
+                    std::lock_guard<std::mutex> lk(mu);
+                    r->state = SID_REQ_RUNNING;
+                    r->admitted = true;
+                    r->t_admit = Clock::now();
+                    r->view = lane.counters_of(r);
+                    w->active.push_back(r);
+                }
+                if(!w->active.empty()) lane.run_step(w->active);
+                std::vector<Request*> done;
+                for(Request* r : w->active) if(lane.queue_size(r) == 0) done.push_back(r);
+                std::vector<sid::ReqDev> final_counts;
+                for(Request* r : done) {
+                    lane.fetch_criticals(r);
+                    final_counts.push_back(lane.counters_of(r));
+                    lane.release(r);
+                    held.erase(std::find(held.begin(), held.end(), r));
+                }
+                std::lock_guard<std::mutex> lk(mu);
+                mem_used += std::uint64_t(std::max<long long>(0, lane.take_grown_bytes()));
+                for(Request* r : w->active) if(r->slot >= 0) r->view = lane.counters_of(r);
+                for(std::size_t i = 0; i < done.size(); ++i) {
+                    Request* r = done[i];
+                    r->view = final_counts[i];
+                    mem_used -= std::min(mem_used, r->bytes);
+                    r->state = SID_REQ_DONE;
+                    r->t_done = Clock::now();
+                    w->active.erase(std::find(w->active.begin(), w->active.end(), r));
+                }
+                if(!done.empty()) cv_done.notify_all();
+            }
+        } catch(const SidError& e) {
+            fail_all(*w, e.msg);
+        } catch(const std::exception& e) {
+            fail_all(*w, e.what());
+        }
+        if(w->lane) {
+            for(Request* r : held) w->lane->release(r);
+            w->lane.reset();
+        }
+    }
+
+    static void fill_status(const Request& r, sid_request_status* st) {
+        std::memset(st, 0, sizeof(*st));
+        st->state = r.state;
+        st->num_cuboids = r.view.cnt[RC_CUBOIDS];
+        st->num_leaf_cuboids = r.view.cnt[RC_LEAVES];
+        st->num_critical_cuboids = r.view.cnt[RC_CRITICALS];
+        st->escalated = r.view.cnt[RC_ESCALATED];
+        st->criticals_stored = std::min<std::uint64_t>(r.view.cnt[RC_CRITICALS], r.crit_cap);
+        st->proved = r.state == SID_REQ_DONE && r.view.cnt[RC_CRITICALS] == 0;
+        if(r.admitted) st->seconds_queued = std::chrono::duration<double>(r.t_admit - r.t_submit).count();
+        if(r.state == SID_REQ_DONE || r.state == SID_REQ_FAILED) {
+            st->seconds_to_verdict = std::chrono::duration<double>(r.t_done - r.t_submit).count();
+        }
+    }
+};
 
 namespace sid {
 
@@ -652,6 +1031,7 @@ void sid_engine_destroy(sid_engine* engine) {
     {
         std::unique_ptr<sid_engine> owner(engine);
         cudaStream_t s = engine->stream;
+        engine->prove_lanes.clear();
         engine->lemmas.clear();
         owner.reset();
         if(s) cudaStreamDestroy(s);
@@ -706,18 +1086,15 @@ int sid_lemma_root_box(sid_engine* engine, int lemma_id, double* out_lohi) {
 
 int sid_prove(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, sid_result* result) {
     return guarded([&] {
-        Lemma* l = get_lemma(engine, lemma_id);
+        get_lemma(engine, lemma_id);
         if(!result) fail(SID_ERR_INVALID, "null result");
         sid_prove_opts o;
         if(opts) o = *opts; else sid_prove_opts_default(&o);
-        if(o.precision != SID_PRECISION_PLAIN && o.precision != SID_PRECISION_FP32_ESCALATE) {
-            fail(SID_ERR_INVALID, "unknown precision mode %d", o.precision);
-        }
+        check_precision(o.precision);
         if(o.generation_count > 250) fail(SID_ERR_INVALID, "generation_count too large");
         set_device(engine);
         std::memset(result, 0, sizeof(*result));
-        Prover p(engine, l, o);
-        p.run(result);
+        prove_one(engine, lemma_id, o, result);
     });
 }
 
@@ -768,6 +1145,143 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
         cuda_check(cudaMemcpyAsync(out_hi, engine->batch_out_hi.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaMemcpyAsync(verdict, engine->batch_verdict.p, std::size_t(n), cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaStreamSynchronize(s), "eval batch sync");
+    });
+}
+
+void sid_server_opts_default(sid_server_opts* o) {
+    if(!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->memory_budget_bytes = std::uint64_t(16) << 30;
+    o->step_elements = std::int64_t(kDefaultStep);
+    o->precision = SID_PRECISION_FP32_ESCALATE;
+    o->generation_count = 8;
+    o->max_criticals_per_request = 1024;
+    o->max_requests_per_lane = kDefaultSlots;
+}
+
+int sid_server_create(sid_engine* engine, const sid_server_opts* opts, sid_server** out) {
+    return guarded([&] {
+        if(!engine || !out) fail(SID_ERR_INVALID, "null argument");
+        auto s = std::make_unique<sid_server>();
+        s->eng = engine;
+        if(opts) s->opts = *opts; else sid_server_opts_default(&s->opts);
+        check_precision(s->opts.precision);
+        if(s->opts.generation_count == 0) s->opts.generation_count = 8;
+        if(s->opts.generation_count > 250) fail(SID_ERR_INVALID, "generation_count too large");
+        *out = s.release();
+    });
+}
+
+void sid_server_destroy(sid_server* server) {
+    if(!server) return;
+    {
+        std::lock_guard<std::mutex> lk(server->mu);
+        server->stopping = true;
+        for(auto& w : server->workers) w.second->cv.notify_all();
+    }
+    for(auto& w : server->workers) {
+        if(w.second->th.joinable()) w.second->th.join();
+    }
+    delete server;
+}
+
+int sid_submit(sid_server* server, int lemma_id, const double* boxes, uint64_t nboxes, uint64_t* request_id) {
+    return guarded([&] {
+        if(!server || !request_id) fail(SID_ERR_INVALID, "null argument");
+        Lemma* lem = get_lemma(server->eng, lemma_id);
+        if(boxes && nboxes == 0) fail(SID_ERR_INVALID, "empty sub-box request");
+        if(boxes && nboxes > (std::uint64_t(1) << 31)) fail(SID_ERR_INVALID, "too many sub-boxes");
+        auto r = std::make_unique<Request>();
+        r->lem = lem;
+        r->lemma_id = lemma_id;
+        r->full = boxes == nullptr;
+        if(boxes) {
+            r->nboxes = nboxes;
+            r->boxes.assign(boxes, boxes + 2 * nboxes * std::uint64_t(lem->ir.nargs));
+            for(std::uint64_t i = 0; i < nboxes * std::uint64_t(lem->ir.nargs); ++i) {
+                const double lo = r->boxes[std::size_t(2 * i)], hi = r->boxes[std::size_t(2 * i + 1)];
+                if(!(lo <= hi)) fail(SID_ERR_INVALID, "sub-box %llu has an empty or NaN range",
+                                     (unsigned long long)(i / std::uint64_t(lem->ir.nargs)));
+            }
+        }
+        r->generations = server->opts.generation_count;
+        r->crit_cap = server->opts.max_criticals_per_request;
+        r->t_submit = Clock::now();
+        std::lock_guard<std::mutex> lk(server->mu);
+        if(server->stopping) fail(SID_ERR_INVALID, "server is stopping");
+        r->id = server->next_id++;
+        Request* raw = r.get();
+        server->reqs[r->id] = std::move(r);
+        auto& w = server->workers[lemma_id];
+        if(!w) {
+            w.reset(new sid_server::Worker);
+            w->lemma_id = lemma_id;
+            sid_server::Worker* wp = w.get();
+            w->th = std::thread([server, wp] { server->worker_loop(wp); });
+        }
+        w->pending.push_back(raw);
+        w->cv.notify_all();
+        *request_id = raw->id;
+    });
+}
+
+int sid_request_poll(sid_server* server, uint64_t request_id, sid_request_status* status) {
+    return guarded([&] {
+        if(!server || !status) fail(SID_ERR_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(server->mu);
+        auto it = server->reqs.find(request_id);
+        if(it == server->reqs.end()) fail(SID_ERR_INVALID, "unknown request %llu", (unsigned long long)request_id);
+        sid_server::fill_status(*it->second, status);
+        if(it->second->state == SID_REQ_FAILED) fail(SID_ERR_CUDA, "request failed: %s", it->second->error.c_str());
+    });
+}
+
+int sid_request_wait(sid_server* server, uint64_t request_id, int timeout_ms, sid_request_status* status) {
+    return guarded([&] {
+        if(!server || !status) fail(SID_ERR_INVALID, "null argument");
+        std::unique_lock<std::mutex> lk(server->mu);
+        auto it = server->reqs.find(request_id);
+        if(it == server->reqs.end()) fail(SID_ERR_INVALID, "unknown request %llu", (unsigned long long)request_id);
+        Request* r = it->second.get();
+        auto finished = [&] { return r->state == SID_REQ_DONE || r->state == SID_REQ_FAILED; };
+        if(timeout_ms < 0) server->cv_done.wait(lk, finished);
+        else server->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished);
+        sid_server::fill_status(*r, status);
+        if(r->state == SID_REQ_FAILED) fail(SID_ERR_CUDA, "request failed: %s", r->error.c_str());
+        if(!finished()) fail(SID_ERR_TIMEOUT, "request %llu not finished after %d ms", (unsigned long long)request_id,
+                             timeout_ms);
+    });
+}
+
+int sid_request_criticals(sid_server* server, uint64_t request_id, double* out, uint64_t capacity, uint64_t* n_out) {
+    return guarded([&] {
+        if(!server) fail(SID_ERR_INVALID, "null server");
+        std::lock_guard<std::mutex> lk(server->mu);
+        auto it = server->reqs.find(request_id);
+        if(it == server->reqs.end()) fail(SID_ERR_INVALID, "unknown request %llu", (unsigned long long)request_id);
+        Request* r = it->second.get();
+        if(r->state != SID_REQ_DONE) fail(SID_ERR_INVALID, "request %llu has not finished", (unsigned long long)request_id);
+        const std::uint64_t per = 2 * std::uint64_t(r->lem->ir.nargs);
+        const std::uint64_t have = r->criticals.size() / per;
+        const std::uint64_t n = std::min(have, capacity);
+        if(n && !out) fail(SID_ERR_INVALID, "null output");
+        if(n) std::memcpy(out, r->criticals.data(), n * per * sizeof(double));
+        if(n_out) *n_out = n;
+        if(have > capacity) fail(SID_ERR_CAPACITY, "%llu criticals stored, capacity %llu",
+                                 (unsigned long long)have, (unsigned long long)capacity);
+    });
+}
+
+int sid_request_release(sid_server* server, uint64_t request_id) {
+    return guarded([&] {
+        if(!server) fail(SID_ERR_INVALID, "null server");
+        std::lock_guard<std::mutex> lk(server->mu);
+        auto it = server->reqs.find(request_id);
+        if(it == server->reqs.end()) fail(SID_ERR_INVALID, "unknown request %llu", (unsigned long long)request_id);
+        const int st = it->second->state;
+        if(st != SID_REQ_DONE && st != SID_REQ_FAILED) fail(SID_ERR_INVALID, "request %llu has not finished",
+                                                            (unsigned long long)request_id);
+        server->reqs.erase(it);
     });
 }
 

@@ -22,6 +22,30 @@ namespace sid {
 
 enum BoundResult : int { B_NONE = 0, B_LB = 1, B_UB = 2, B_BOTH = 3, B_EMPTY = 4 };
 
+/// Per-request counters on the device (indices into ReqDev::cnt).
+enum ReqCounter : int {
+    RC_CUBOIDS = 0,      // cuboids considered
+    RC_LEAVES = 1,       // leaf cuboids
+    RC_CRITICALS = 2,    // critical cuboids (final generation)
+    RC_ESCALATED = 3,    // precision form: children evaluated in double
+    RC_QSIZE = 4,        // elements in the request's queue (appended with atomics)
+    RC_OVERFLOW = 5,     // a queue append did not fit (the host sizes queues so that this stays 0)
+    RC_N = 6
+};
+
+/// Device state of one request (a proof, or a set of sub-boxes of a lemma): counters, its frontier queue
+/// (a LIFO stack: nargs columns of qcap double2 plus a depth byte) and its critical-box store.
+struct ReqDev {
+    unsigned long long cnt[RC_N];
+    double2* qbox;
+    std::uint8_t* qdepth;
+    unsigned long long qcap;
+    double* crit;                      // 2*nargs doubles per stored critical
+    unsigned long long crit_cap;
+    unsigned int generations;          // elements of depth >= generations are final
+    unsigned int pad;
+};
+
 /// Applies a bound function value v to the target interval (CompileTimeBound::apply_to,
 /// constraints_to_bounds/compile_time_bound.hpp:42-85).
 template<int DIR, bool DEFINED, class T> __device__ __forceinline__ int apply_to(Iv<T>& t, const Iv<T>& v) {
@@ -152,38 +176,88 @@ struct LevelArgs {
     const std::uint8_t* in_depth;     // depth of each item (MODE_QUEUE; nullptr: depth_value)
     std::uint64_t in_begin, n_in;     // items [in_begin, in_begin + n_in)
     std::uint32_t elem_base;
+    // request of each item: in_tag[item], else elem_tag[element], else tag_value
+    const std::uint32_t* in_tag;
+    const std::uint32_t* elem_tag;
+    std::uint32_t tag_value;
+    ReqDev* req;                      // per-request counters, queues (MODE_QUEUE), critical stores
+    bool count_cuboids;               // every child counts as one cuboid of its request
     int var, nsub, it_limit, rec_limit;
     int row_begin, row_end;           // constraint rows to test (row_end <= row_begin: none)
     std::uint8_t depth_value;         // depth for MODE_QUEUE when in_depth is null
     std::uint8_t depth_add;           // added to the input depth for MODE_QUEUE
-    // outputs (MODE_EMIT / MODE_QUEUE)
+    // outputs (MODE_EMIT; MODE_QUEUE appends to the request's queue instead)
     double2* out_box;
     std::uint64_t out_stride, out_cap;
     std::uint32_t* out_elem;
     std::uint64_t* out_path;
     std::uint8_t* out_depth;
+    std::uint32_t* out_tag;
     unsigned long long* out_count;    // slots already used on entry
     // hull (MODE_HULL): per element and variable
     unsigned long long* hull_lo;      // order keys, min
     unsigned long long* hull_hi;      // order keys, max
     unsigned long long* hull_zlo;     // (path<<1 | sign) of the first leaf whose lo is zero
     unsigned long long* hull_zhi;
-    // criticals (MODE_CRIT): 2*nargs doubles each
-    double* crit;
-    std::uint64_t crit_cap;
-    unsigned long long* crit_count;
-    // counters
-    unsigned long long* leaf_count;
     unsigned int* overflow;           // set when an output list would overflow
     // precision form (k_filter_f32 / k_level_esc): children [child_begin, child_begin + n_child) of
     // the items, the escalation list (child ids relative to child_begin) and its length
     std::uint64_t child_begin, n_child;
     std::uint32_t* esc;
     unsigned long long* esc_count;
-    unsigned long long* esc_total;    // escalated children over the whole proof
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanes_below() { return (1u << lane_id()) - 1u; }
+
+__device__ __forceinline__ std::uint32_t item_elem(const LevelArgs& a, std::uint64_t item) {
+    return a.in_elem ? a.in_elem[item] : std::uint32_t(item - a.in_begin) + a.elem_base;
+}
+__device__ __forceinline__ std::uint32_t item_tag(const LevelArgs& a, std::uint64_t item) {
+    return a.in_tag ? a.in_tag[item] : (a.elem_tag ? a.elem_tag[item_elem(a, item)] : a.tag_value);
+}
+
+/// Adds per-lane values to the counters F0, F1, F2 (-1: unused) of each lane's request: one atomic per
+/// distinct request among the lanes of `active` (all of which call this together, with uniform masks).
+template<int F0, int F1, int F2>
+__device__ __forceinline__ void add_to_requests(unsigned active, ReqDev* req, std::uint32_t tag, unsigned v0, unsigned v1,
+                                                unsigned v2) {
+    unsigned pending = active;
+    while(pending) {
+        const int leader = __ffs(pending) - 1;
+        const std::uint32_t t = __shfl_sync(active, tag, leader);
+        const bool mine = tag == t;
+        const unsigned grp = __ballot_sync(active, mine);
+        const unsigned s0 = F0 >= 0 ? __reduce_add_sync(active, mine ? v0 : 0u) : 0u;
+        const unsigned s1 = F1 >= 0 ? __reduce_add_sync(active, mine ? v1 : 0u) : 0u;
+        const unsigned s2 = F2 >= 0 ? __reduce_add_sync(active, mine ? v2 : 0u) : 0u;
+        if(int(lane_id()) == leader) {
+            if(F0 >= 0 && s0) atomicAdd(&req[t].cnt[F0 >= 0 ? F0 : 0], (unsigned long long)s0);
+            if(F1 >= 0 && s1) atomicAdd(&req[t].cnt[F1 >= 0 ? F1 : 0], (unsigned long long)s1);
+            if(F2 >= 0 && s2) atomicAdd(&req[t].cnt[F2 >= 0 ? F2 : 0], (unsigned long long)s2);
+        }
+        pending &= ~grp;
+    }
+}
+
+/// Reserves queue slots in each lane's request for the lanes with `want` set (one atomic per request).
+__device__ __forceinline__ unsigned long long reserve_queue_slots(unsigned active, ReqDev* req, std::uint32_t tag, bool want) {
+    unsigned pending = active;
+    unsigned long long slot = 0;
+    while(pending) {
+        const int leader = __ffs(pending) - 1;
+        const std::uint32_t t = __shfl_sync(active, tag, leader);
+        const bool mine = tag == t;
+        const unsigned grp = __ballot_sync(active, mine);
+        const unsigned m = __ballot_sync(active, mine && want);
+        unsigned long long base = 0;
+        if(int(lane_id()) == leader && m) base = atomicAdd(&req[t].cnt[RC_QSIZE], (unsigned long long)__popc(m));
+        base = __shfl_sync(active, base, leader);
+        if(mine && want) slot = base + __popc(m & lanes_below());
+        pending &= ~grp;
+    }
+    return slot;
+}
 
 /// One child c of item `item`: split, propagate, test rows, then emit / join / store. All lanes of
 /// `active` call this together (warp-aggregated atomics).
@@ -204,40 +278,50 @@ __device__ __forceinline__ void level_child(const LevelArgs& a, const std::uint6
     bool ok = !propagate<L, T>(a.var, box, a.it_limit, a.rec_limit);
     if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<T>(a.row_begin, a.row_end, box);
 
-    unsigned long long leaves = ok ? 0ull : 1ull;
-    if(MODE == MODE_HULL || MODE == MODE_CRIT) leaves = 1ull;
+    const unsigned leaves = (MODE == MODE_HULL || MODE == MODE_CRIT) ? 1u : (ok ? 0u : 1u);
+    const std::uint32_t tag = item_tag(a, item);
 
-    if(MODE == MODE_EMIT || MODE == MODE_QUEUE) {
+    if(MODE == MODE_EMIT) {
         const unsigned m = __ballot_sync(active, ok);
         const int leader = __ffs(active) - 1;
         unsigned long long base = 0;
         if(int(lane_id()) == leader && m) base = atomicAdd(a.out_count, (unsigned long long)__popc(m));
         base = __shfl_sync(active, base, leader);
         if(ok) {
-            const std::uint64_t slot = base + __popc(m & ((1u << lane_id()) - 1u));
+            const std::uint64_t slot = base + __popc(m & lanes_below());
             if(slot < a.out_cap) {
                 #pragma unroll
                 for(int v = 0; v < N; ++v) {
                     a.out_box[std::uint64_t(v) * a.out_stride + slot] = make_double2(double(box[v].lo), double(box[v].hi));
                 }
-                if(MODE == MODE_EMIT && a.out_elem) {
-                    a.out_elem[slot] = a.in_elem ? a.in_elem[item] : std::uint32_t(item - a.in_begin) + a.elem_base;
-                }
-                if(MODE == MODE_EMIT && a.out_path) {
+                if(a.out_elem) a.out_elem[slot] = item_elem(a, item);
+                if(a.out_path) {
                     std::uint64_t p = a.in_path ? a.in_path[item] : 0ull;
                     a.out_path[slot] = p * std::uint64_t(a.nsub) + std::uint64_t(c);
                 }
-                if(a.out_depth) {
-                    std::uint8_t d = a.in_depth ? a.in_depth[item] : a.depth_value;
-                    a.out_depth[slot] = std::uint8_t(d + (MODE == MODE_QUEUE ? a.depth_add : 0));
-                }
+                if(a.out_depth) a.out_depth[slot] = a.in_depth ? a.in_depth[item] : a.depth_value;
+                if(a.out_tag) a.out_tag[slot] = tag;
             } else {
                 atomicOr(a.overflow, 1u);
             }
         }
+    } else if(MODE == MODE_QUEUE) {
+        const unsigned long long slot = reserve_queue_slots(active, a.req, tag, ok);
+        if(ok) {
+            ReqDev* r = a.req + tag;
+            const unsigned long long cap = r->qcap;
+            if(slot < cap) {
+                #pragma unroll
+                for(int v = 0; v < N; ++v) r->qbox[std::uint64_t(v) * cap + slot] = make_double2(double(box[v].lo), double(box[v].hi));
+                const std::uint8_t d = a.in_depth ? a.in_depth[item] : a.depth_value;
+                r->qdepth[slot] = std::uint8_t(d + a.depth_add);
+            } else {
+                atomicAdd(&r->cnt[RC_OVERFLOW], 1ull);
+            }
+        }
     } else if(MODE == MODE_HULL) {
         if(ok) {
-            const std::uint32_t e = a.in_elem ? a.in_elem[item] : std::uint32_t(item - a.in_begin) + a.elem_base;
+            const std::uint32_t e = item_elem(a, item);
             const std::uint64_t path = (a.in_path ? a.in_path[item] : 0ull) * std::uint64_t(a.nsub) + std::uint64_t(c);
             #pragma unroll
             for(int v = 0; v < N; ++v) {
@@ -251,20 +335,19 @@ __device__ __forceinline__ void level_child(const LevelArgs& a, const std::uint6
         }
     } else if(MODE == MODE_CRIT) {
         if(ok) {
-            const unsigned long long slot = atomicAdd(a.crit_count, 1ull);
-            if(slot < a.crit_cap) {
+            ReqDev* r = a.req + tag;
+            const unsigned long long slot = atomicAdd(&r->cnt[RC_CRITICALS], 1ull);
+            if(slot < r->crit_cap) {
                 #pragma unroll
                 for(int v = 0; v < N; ++v) {
-                    a.crit[(slot * N + v) * 2] = double(box[v].lo);
-                    a.crit[(slot * N + v) * 2 + 1] = double(box[v].hi);
+                    r->crit[(slot * N + v) * 2] = double(box[v].lo);
+                    r->crit[(slot * N + v) * 2 + 1] = double(box[v].hi);
                 }
             }
         }
     }
 
-    // warp-aggregated leaf count (each thread contributes at most one leaf)
-    const unsigned wsum = __reduce_add_sync(active, unsigned(leaves));
-    if(int(lane_id()) == __ffs(active) - 1 && wsum) atomicAdd(a.leaf_count, (unsigned long long)wsum);
+    add_to_requests<RC_CUBOIDS, RC_LEAVES, -1>(active, a.req, tag, a.count_cuboids ? 1u : 0u, leaves, 0u);
 }
 
 template<class L, class T, int MODE> __global__ void __launch_bounds__(128) k_level(const LevelArgs a) {
@@ -300,14 +383,10 @@ template<class L> __global__ void __launch_bounds__(128) k_filter_f32(const Leve
     const unsigned m = __ballot_sync(active, ok);
     const int leader = __ffs(active) - 1;
     unsigned long long base = 0;
-    if(int(lane_id()) == leader && m) {
-        base = atomicAdd(a.esc_count, (unsigned long long)__popc(m));
-        atomicAdd(a.esc_total, (unsigned long long)__popc(m));
-    }
+    if(int(lane_id()) == leader && m) base = atomicAdd(a.esc_count, (unsigned long long)__popc(m));
     base = __shfl_sync(active, base, leader);
-    if(ok) a.esc[base + __popc(m & ((1u << lane_id()) - 1u))] = std::uint32_t(t);
-    const unsigned refuted = __popc(active & ~m);
-    if(int(lane_id()) == leader && refuted) atomicAdd(a.leaf_count, (unsigned long long)refuted);
+    if(ok) a.esc[base + __popc(m & lanes_below())] = std::uint32_t(t);
+    add_to_requests<RC_CUBOIDS, RC_LEAVES, RC_ESCALATED>(active, a.req, item_tag(a, item), 1u, ok ? 0u : 1u, ok ? 1u : 0u);
 }
 
 /// Precision form, second pass: the escalated children, in double, with the plain form's outputs.

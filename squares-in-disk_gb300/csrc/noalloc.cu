@@ -22,8 +22,10 @@ using namespace sid;
 // 8 MiB per device, held from library load until process exit.
 constexpr std::size_t kScratchBytes = std::size_t(8) << 20;
 constexpr std::size_t kScratchWords = kScratchBytes / sizeof(unsigned long long);
-// header: word 0 leaf counter, words 1..2 unused counters of the level kernel; keys start at word 32
+// header: words 0..11 the request record the level kernel counts into (ReqDev: word 1 = leaves),
+// word 16 the list-overflow flag; keys start at word 32
 constexpr std::size_t kHeaderWords = 32;
+static_assert(sizeof(ReqDev) <= 16 * sizeof(unsigned long long), "request record must fit the header");
 // four accumulator arrays (lo key, hi key, first-zero lo, first-zero hi) of n * nargs words each
 constexpr std::uint64_t kMaxItemVars = (kScratchWords - kHeaderWords) / 4;
 
@@ -37,7 +39,7 @@ unsigned long long* g_scratch_addr[kMaxDevices] = {};
 __global__ void k_leaf_hull_decode(const unsigned long long* scratch, std::uint64_t n, int nargs, double2* hulls,
                                    std::uint8_t* nonempty, unsigned long long* leaves_out) {
     const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if(i == 0 && leaves_out) *leaves_out = scratch[0];
+    if(i == 0 && leaves_out) *leaves_out = reinterpret_cast<const ReqDev*>(scratch)->cnt[RC_LEAVES];
     if(i >= n) return;
     const std::uint64_t m = n * std::uint64_t(nargs);
     const unsigned long long* lo = scratch + kHeaderWords;
@@ -130,9 +132,10 @@ extern "C" int sid_leaf_hull_noalloc(sid_engine* engine, int lemma_id, const dou
     a.rec_limit = 4;
     a.row_begin = view.last_static_arg;
     a.row_end = view.nargs;
-    a.leaf_count = scratch;
-    a.overflow = reinterpret_cast<unsigned int*>(scratch + 1);
-    a.crit_count = scratch + 2;
+    a.req = reinterpret_cast<ReqDev*>(scratch);   // one request, tag 0, zeroed above
+    a.tag_value = 0;
+    a.count_cuboids = false;
+    a.overflow = reinterpret_cast<unsigned int*>(scratch + 16);
     a.hull_lo = lo;
     a.hull_hi = lo + m;
     a.hull_zlo = lo + 2 * m;

@@ -21,7 +21,12 @@ STATUS = {0: "ok", -1: "invalid", -2: "cuda", -3: "not_compiled", -4: "nomem", -
 
 EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "sid_engine_destroy",
             "sid_lemma_register", "sid_lemma_info", "sid_lemma_root_box", "sid_prove", "sid_fetch_criticals",
-            "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc"]
+            "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc", "sid_server_opts_default",
+            "sid_server_create", "sid_server_destroy", "sid_submit", "sid_request_poll", "sid_request_wait",
+            "sid_request_criticals", "sid_request_release"]
+
+PRECISION_PLAIN, PRECISION_FP32 = 0, 1
+REQ_PENDING, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 
 class SidResult(ctypes.Structure):
@@ -41,6 +46,25 @@ class SidProveOpts(ctypes.Structure):
                 ("max_criticals_kept", ctypes.c_uint64), ("progress", ctypes.c_void_p),
                 ("progress_user", ctypes.c_void_p), ("progress_first_ms", ctypes.c_uint32),
                 ("progress_every_ms", ctypes.c_uint32)]
+
+
+class SidServerOpts(ctypes.Structure):
+    _fields_ = [("memory_budget_bytes", ctypes.c_uint64), ("step_elements", ctypes.c_int64),
+                ("precision", ctypes.c_int32), ("generation_count", ctypes.c_uint32),
+                ("max_criticals_per_request", ctypes.c_uint64), ("max_requests_per_lane", ctypes.c_uint32)]
+
+
+class SidRequestStatus(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("proved", ctypes.c_int32), ("num_cuboids", ctypes.c_uint64),
+                ("num_leaf_cuboids", ctypes.c_uint64), ("num_critical_cuboids", ctypes.c_uint64),
+                ("escalated", ctypes.c_uint64), ("criticals_stored", ctypes.c_uint64),
+                ("seconds_queued", ctypes.c_double), ("seconds_to_verdict", ctypes.c_double)]
+
+    def as_dict(self):
+        return dict(state=self.state, proved=bool(self.proved), cuboids=self.num_cuboids,
+                    leaves=self.num_leaf_cuboids, criticals=self.num_critical_cuboids, escalated=self.escalated,
+                    stored=self.criticals_stored, seconds_queued=self.seconds_queued,
+                    seconds_to_verdict=self.seconds_to_verdict)
 
 
 class SidError(RuntimeError):
@@ -77,6 +101,16 @@ def load(path=LIB_PATH):
                                         ctypes.c_void_p]
     L.sid_leaf_hull_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.sid_server_opts_default.argtypes = [ctypes.POINTER(SidServerOpts)]
+    L.sid_server_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(SidServerOpts), ctypes.POINTER(ctypes.c_void_p)]
+    L.sid_server_destroy.argtypes = [ctypes.c_void_p]
+    L.sid_submit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                             ctypes.POINTER(ctypes.c_uint64)]
+    L.sid_request_poll.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(SidRequestStatus)]
+    L.sid_request_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(SidRequestStatus)]
+    L.sid_request_criticals.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                                        ctypes.POINTER(ctypes.c_uint64)]
+    L.sid_request_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
     _lib = L
     return L
 
@@ -186,6 +220,99 @@ class Engine:
         """Allocation-free leaf hulls on caller device buffers (see sid_leaf_hull_noalloc in sid.h)."""
         _check(self.L.sid_leaf_hull_noalloc(self.h, lemma_id, boxes_ptr, n, hulls_ptr, nonempty_ptr, leaves_ptr,
                                             stream))
+
+
+class Server:
+    """The served form (sid_server_*): requests of whole lemmas or sub-boxes, continuously batched per lemma."""
+
+    def __init__(self, engine, precision=PRECISION_FP32, memory_budget=0, step_elements=0, generations=8,
+                 max_criticals=1024, max_requests_per_lane=0):
+        self.engine = engine
+        self.L = engine.L
+        o = SidServerOpts()
+        self.L.sid_server_opts_default(ctypes.byref(o))
+        o.precision = precision
+        if memory_budget:
+            o.memory_budget_bytes = memory_budget
+        if step_elements:
+            o.step_elements = step_elements
+        o.generation_count = generations
+        o.max_criticals_per_request = max_criticals
+        if max_requests_per_lane:
+            o.max_requests_per_lane = max_requests_per_lane
+        h = ctypes.c_void_p()
+        _check(self.L.sid_server_create(engine.h, ctypes.byref(o), ctypes.byref(h)))
+        self.h = h
+        self.nargs = {}
+
+    def close(self):
+        if self.h:
+            self.L.sid_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, lemma_id, boxes=None):
+        """boxes: None for the whole lemma, else an array (nboxes, nargs, 2) of (lo, hi)."""
+        rid = ctypes.c_uint64()
+        if boxes is None:
+            _check(self.L.sid_submit(self.h, lemma_id, None, 0, ctypes.byref(rid)))
+        else:
+            b = np.ascontiguousarray(boxes, dtype=np.float64)
+            self.nargs[rid.value] = b.shape[1]
+            _check(self.L.sid_submit(self.h, lemma_id, b.ctypes.data, b.shape[0], ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, rid):
+        st = SidRequestStatus()
+        _check(self.L.sid_request_poll(self.h, rid, ctypes.byref(st)))
+        return st.as_dict()
+
+    def wait(self, rid, timeout_ms=-1):
+        st = SidRequestStatus()
+        _check(self.L.sid_request_wait(self.h, rid, timeout_ms, ctypes.byref(st)))
+        return st.as_dict()
+
+    def criticals(self, rid, nargs, capacity):
+        buf = np.zeros(max(capacity, 1) * 2 * nargs, dtype=np.float64)
+        got = ctypes.c_uint64()
+        _check(self.L.sid_request_criticals(self.h, rid, buf.ctypes.data, capacity, ctypes.byref(got)))
+        return buf[: got.value * 2 * nargs].reshape(-1, nargs, 2)
+
+    def release(self, rid):
+        _check(self.L.sid_request_release(self.h, rid))
+
+
+def synthetic_request(root, rng, k=None):
+    """A seeded synthetic sub-box request: a region that covers, per coordinate, a uniform fraction in
+    [2^-8, 1] of the root range at a uniform offset, delivered as k sub-boxes (a grid partition of the region;
+    k = 2^j with j uniform in 0..12 unless given). Returns an array (k, nargs, 2)."""
+    nargs = root.shape[0]
+    lo = np.empty(nargs)
+    hi = np.empty(nargs)
+    for v in range(nargs):
+        a, b = float(root[v, 0]), float(root[v, 1])
+        f = rng.uniform(2.0 ** -8, 1.0)
+        w = (b - a) * f
+        off = a + rng.uniform(0.0, 1.0) * (b - a - w)
+        lo[v], hi[v] = off, min(off + w, b)
+    if k is None:
+        k = 1 << int(rng.integers(0, 13))
+    cells = np.ones(nargs, dtype=np.int64)
+    while cells.prod() < k:
+        cells[int(np.argmax((hi - lo) / cells))] *= 2
+    grids = [np.linspace(lo[v], hi[v], cells[v] + 1) for v in range(nargs)]
+    grids = [np.concatenate([g[:-1], [hi[v]]]) for v, g in enumerate(grids)]
+    idx = np.stack(np.meshgrid(*[np.arange(c) for c in cells], indexing="ij"), axis=-1).reshape(-1, nargs)
+    out = np.empty((idx.shape[0], nargs, 2))
+    for v in range(nargs):
+        out[:, v, 0] = grids[v][idx[:, v]]
+        out[:, v, 1] = grids[v][idx[:, v] + 1]
+    return out
 
 
 def synthetic_batch(root, n, seed=0x5EED0001):
