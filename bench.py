@@ -13,8 +13,9 @@ value: cuboids/s with the batch resident in HBM (CUDA events on the launching st
 e2e: the same through the C ABI with host buffers (sid_eval_batch: H2D copy, kernel, D2H copy).
 Extra fields: the full One Subcontainer proof on the GPU; every lemma proved in the plain FP64 form and
 in the precision form (FP32 first pass, FP64 escalation) with cuboids/s, escalation rate and count change
-(lemma_set); the roofline of the batch kernel; the CPU oracle (a restatement of the reference's CPU
-prover) timed on the host cores.
+(lemma_set); the served form under Poisson request streams with p50/p99 time to verdict in both forms
+(serve); the roofline of the batch kernel; the CPU oracle (a restatement of the reference's CPU prover)
+timed on the host cores.
 --impl reference times the reference's CPU algorithm (the oracle port; the reference itself cannot be
 built on the GPU machine) on the same workload with all host threads.
 """
@@ -169,6 +170,73 @@ def prove_lemma_set(eng, sid, repeats=2):
     return out
 
 
+SERVE_RATES = (100.0, 1000.0, 10000.0)   # Poisson arrival rates of synthetic requests (requests/s)
+SERVE_SYNTHETIC = 200                      # synthetic requests per rate
+SERVE_SEED = 0x5E4E0001
+
+
+def _pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) * 1000.0 if xs else None
+
+
+def serve_stream(eng, sid, precision, rates=SERVE_RATES, n_syn=SERVE_SYNTHETIC):
+    """The served form under a request stream: at each rate, the whole lemma set (11 whole-lemma requests,
+    submitted first) and n_syn seeded synthetic sub-box requests with Poisson arrivals (lemma uniform; a
+    region covering a uniform fraction in [2^-8, 1] of each root range at a uniform offset, delivered as
+    2^j sub-boxes, j uniform in 0..12). Reports p50/p99 time to verdict (submission to completion, host
+    clock) and cuboids/s over the stream's wall time. One server per precision form, warmed up first."""
+    names = sid.lemma_names()
+    lids = {n: eng.register(sid.lemma_ir(n)) for n in names}
+    roots = {n: eng.root_box(lids[n], sid.ir_nargs(sid.lemma_ir(n))) for n in names}
+    out = {}
+    with sid.Server(eng, precision=precision) as srv:
+        warm = [srv.submit(lids[n]) for n in names]     # lane set-up and first allocations
+        for rid in warm:
+            srv.wait(rid)
+            srv.release(rid)
+        for rate in rates:
+            rng = np.random.default_rng(SERVE_SEED)
+            syn = []
+            for _ in range(n_syn):
+                n = names[int(rng.integers(len(names)))]
+                syn.append((n, sid.synthetic_request(roots[n], rng)))
+            gaps = rng.exponential(1.0 / rate, n_syn)
+            t0 = time.perf_counter()
+            whole = [(n, srv.submit(lids[n])) for n in names]
+            ids = []
+            t_next = t0
+            for (n, boxes), g in zip(syn, gaps):
+                t_next += g
+                delay = t_next - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ids.append((n, srv.submit(lids[n], boxes)))
+            res_whole = [srv.wait(rid) for _, rid in whole]
+            res_syn = [srv.wait(rid) for _, rid in ids]
+            wall = time.perf_counter() - t0
+            for _, rid in whole + ids:
+                srv.release(rid)
+            lat_syn = [r["seconds_to_verdict"] for r in res_syn]
+            lat_whole = [r["seconds_to_verdict"] for r in res_whole]
+            cub = sum(r["cuboids"] for r in res_whole + res_syn)
+            out["rate_%g" % rate] = {
+                "offered_rate_per_s": rate, "requests": len(res_whole) + len(res_syn),
+                "synthetic_p50_ms": _pct(lat_syn, 50), "synthetic_p99_ms": _pct(lat_syn, 99),
+                "whole_lemma_p50_ms": _pct(lat_whole, 50), "whole_lemma_p99_ms": _pct(lat_whole, 99),
+                "all_p50_ms": _pct(lat_syn + lat_whole, 50), "all_p99_ms": _pct(lat_syn + lat_whole, 99),
+                "cuboids": cub, "wall_s": wall, "cuboids_per_s": cub / wall,
+                "whole_lemmas_proved": sum(1 for r in res_whole if r["proved"]),
+                "whole_lemma_counts_match_published": None,
+                "synthetic_proved": sum(1 for r in res_syn if r["proved"]),
+                "subboxes": int(sum(len(b) for _, b in syn))}
+            with open(PUBLISHED) as f:
+                pub = json.load(f)
+            if precision == PRECISION_PLAIN:
+                out["rate_%g" % rate]["whole_lemma_counts_match_published"] = all(
+                    [r["cuboids"], r["leaves"]] == pub[n] for (n, _), r in zip(whole, res_whole))
+    return out
+
+
 def run_reference(args):
     _, rank, world, _ = dist_setup()
     if rank != 0:
@@ -289,6 +357,11 @@ def run_ours(args):
     proofs = [eng.prove(lid) for _ in range(3)]
     best = min(proofs, key=lambda r: r["seconds"])
     lemma_set = prove_lemma_set(eng, sid) if not args.no_lemma_set else None
+    serve = None
+    if not args.no_serve:
+        serve = {"fp32": serve_stream(eng, sid, PRECISION_FP32), "plain": serve_stream(eng, sid, PRECISION_PLAIN),
+                 "workload": "whole lemma set + %d seeded synthetic sub-box requests per rate, Poisson arrivals"
+                             % SERVE_SYNTHETIC}
 
     if rank != 0:
         return 0
@@ -316,6 +389,8 @@ def run_ours(args):
     }
     if lemma_set:
         line["lemma_set"] = lemma_set
+    if serve:
+        line["serve"] = serve
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sample, dt = cpu_baseline(ir, lo, hi, threads)
@@ -336,6 +411,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-lemma-set", action="store_true", help="skip the full-proof lemma set")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-form request stream")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

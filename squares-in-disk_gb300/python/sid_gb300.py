@@ -330,3 +330,31 @@ def synthetic_batch(root, n, seed=0x5EED0001):
         lo[v] = l
         hi[v] = np.minimum(l + w, b)
     return lo, hi
+
+
+def main(argv=None):
+    """Command line: prove a lemma once or more on GPU 0 and print the counts.
+
+      python sid_gb300.py prove <lemma> [--precision 0|1] [--repeat N] [--generations G]
+    """
+    import argparse
+    ap = argparse.ArgumentParser(prog="sid_gb300.py")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    p = sub.add_parser("prove")
+    p.add_argument("lemma")
+    p.add_argument("--precision", type=int, default=PRECISION_PLAIN)
+    p.add_argument("--repeat", type=int, default=1)
+    p.add_argument("--generations", type=int, default=8)
+    args = ap.parse_args(argv)
+    eng = Engine(0)
+    lid = eng.register(lemma_ir(args.lemma))
+    for _ in range(args.repeat):
+        r = eng.prove(lid, generations=args.generations, precision=args.precision)
+        print(args.lemma, "precision", args.precision, r, flush=True)
+    eng.close()
+    return 0
+
+
+if __name__ == "__main__":
+    import sys
+    sys.exit(main())
