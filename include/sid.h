@@ -119,9 +119,23 @@ int sid_fetch_criticals(sid_engine* engine, int lemma_id, double* out, uint64_t 
 int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
                    double* out_lo, double* out_hi, int8_t* verdict);
 
-/* Same on device buffers, asynchronous on `stream` (a cudaStream_t; NULL for the legacy stream). */
+/* Same on device buffers, asynchronous on `stream` (a cudaStream_t; NULL for the legacy stream).
+ * Within each tile of 2^18 consecutive cuboids the evaluation follows the Morton order of their lower
+ * corners (computed on the device from the lemma's root box), which keeps a warp's cuboids on the same
+ * code paths; every result is written to its cuboid's own position, so the output does not depend on the
+ * order. The ordering scratch belongs to the engine: calls on one engine must not overlap on different
+ * streams. */
 int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
                           double* out_lo, double* out_hi, int8_t* verdict, void* stream);
+
+/* Kernel timing of the batch calls, for roofline measurements (no counterpart in the reference).
+ * sid_eval_batch_profile(engine, 1) makes every following sid_eval_batch* call record CUDA events on its
+ * stream around its evaluation kernel and around its ordering kernel; sid_eval_batch_profile_read waits
+ * for the recorded events, returns the
+ * number of calls and the summed device milliseconds of the ordering work and of the evaluation kernel,
+ * and clears the record (recording continues until sid_eval_batch_profile(engine, 0)). */
+int sid_eval_batch_profile(sid_engine* engine, int enable);
+int sid_eval_batch_profile_read(sid_engine* engine, uint64_t* calls, double* order_ms, double* eval_ms);
 
 /* Allocation-free leaf hulls. No counterpart in the reference: it is an addition of this library.
  *

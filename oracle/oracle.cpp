@@ -527,15 +527,29 @@ template<class T> struct Driver {
         queue = std::move(out);
     }
 
-    /// Precision form: true if the float evaluation of this child (its box rounded outward to float,
-    /// then the same propagation and constraint rows as the double path) already refutes it.
-    bool refuted_in_fp32(Provers<T>& S, Counts& c, const std::vector<Iv<T>>& child, int arg, std::size_t it,
-                         unsigned rec, int r0, int r1) {
+    /// Precision form: true if the float evaluation of child i of `parent` split n ways on `arg` already
+    /// refutes it: the parent box rounded outward to float, the split variable's child range formed in
+    /// float from RD(lb), RU(lb), RD(w), RU(w), RU(ub) with w = (ub - lb) / n in double (a float range
+    /// that contains the double child range: lo = RD(RD(lb) + RD(i*RD(w))), hi = RU(RU(lb) + RU((i+1)*RU(w))),
+    /// the last child ending at RU(ub)), then the same propagation and constraint rows as the double path.
+    bool refuted_in_fp32(Provers<T>& S, Counts& c, const std::vector<Iv<T>>& parent, int arg, int i, int n,
+                         std::size_t it, unsigned rec, int r0, int r1) {
         if(!S.F) return false;
         std::vector<Iv<float>>& fb = fbox;
-        fb.resize(child.size());
-        for(std::size_t v = 0; v < child.size(); ++v) {
-            fb[v] = {static_cast<float>(child[v].lo), -static_cast<float>(-child[v].hi), false};   // round-down mode
+        fb.resize(parent.size());
+        // the ambient rounding mode is downward: a cast rounds down, -cast(-x) rounds up
+        for(std::size_t v = 0; v < parent.size(); ++v) {
+            fb[v] = {static_cast<float>(parent[v].lo), -static_cast<float>(-parent[v].hi), false};
+        }
+        {
+            const T lb = parent[std::size_t(arg)].lo, ub = parent[std::size_t(arg)].hi;
+            const T w = (ub - lb) / T(n);
+            const float lb_lo = static_cast<float>(lb), lb_hi = -static_cast<float>(-lb);
+            const float w_lo = static_cast<float>(w), w_hi = -static_cast<float>(-w);
+            const float ub_hi = -static_cast<float>(-ub);
+            const float lo = lb_lo + float(i) * w_lo;
+            const float hi = (i + 1 >= n) ? ub_hi : -((-lb_hi) - (-(-float(i + 1) * w_hi)));
+            fb[std::size_t(arg)] = {lo, hi, false};
         }
         bool refuted = S.F->propagate(arg, fb.data(), it, rec) || (r1 > r0 && !S.F->rows_ok(r0, r1, fb.data()));
         if(refuted) ++c.fp32_refuted; else ++c.escalated;
@@ -558,8 +572,11 @@ template<class T> struct Driver {
             T lo, hi;
             split_point_pair(box[std::size_t(s.arg)].lo, box[std::size_t(s.arg)].hi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
-            if(refuted_in_fp32(S, c, child, s.arg, 2 * std::size_t(L.nargs), rec_limit, d + 1 == dyn.size() ? L.nargs - 1 : 0,
-                               d + 1 == dyn.size() ? L.nargs : 0)) { ++c.leaves; continue; }
+            if(refuted_in_fp32(S, c, box, s.arg, i, m, 2 * std::size_t(L.nargs), rec_limit,
+                               d + 1 == dyn.size() ? L.nargs - 1 : 0, d + 1 == dyn.size() ? L.nargs : 0)) {
+                ++c.leaves;
+                continue;
+            }
             if(P.propagate(s.arg, child.data(), 2 * L.nargs, rec_limit)) { ++c.leaves; continue; }
             init_rec(S, c, d + 1, child, rec_limit, out);
         }
@@ -603,7 +620,7 @@ template<class T> struct Driver {
             T lo, hi;
             split_point_pair(plo, phi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
-            if(refuted_in_fp32(S, c, child, s.arg, std::size_t(L.nargs), 4, r0, r1)) { ++c.leaves; continue; }
+            if(refuted_in_fp32(S, c, box, s.arg, i, m, std::size_t(L.nargs), 4, r0, r1)) { ++c.leaves; continue; }
             if(P.propagate(s.arg, child.data(), std::size_t(L.nargs), 4)) { ++c.leaves; continue; }
             if(!P.rows_ok(r0, r1, child.data())) { ++c.leaves; continue; }
             handle(S, c, j + 1, child, hull);
@@ -642,8 +659,11 @@ template<class T> struct Driver {
             T lo, hi;
             split_point_pair(box[std::size_t(s.arg)].lo, box[std::size_t(s.arg)].hi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
-            if(refuted_in_fp32(S, c, child, s.arg, 2 * std::size_t(L.nargs), rec_limit, d + 1 == dyn.size() ? L.nargs - 1 : 0,
-                               d + 1 == dyn.size() ? L.nargs : 0)) { ++c.leaves; continue; }
+            if(refuted_in_fp32(S, c, box, s.arg, i, m, 2 * std::size_t(L.nargs), rec_limit,
+                               d + 1 == dyn.size() ? L.nargs - 1 : 0, d + 1 == dyn.size() ? L.nargs : 0)) {
+                ++c.leaves;
+                continue;
+            }
             if(P.propagate(s.arg, child.data(), 2 * L.nargs, rec_limit)) { ++c.leaves; continue; }
             split_rec(S, c, d + 1, child, depth, out);
         }

@@ -156,6 +156,7 @@ struct Lemma {
     sid::LemmaIR ir;
     const sid::LemmaKernels* k = nullptr;
     DevBuf<double2> root;                // initial runtime box, computed once at registration
+    std::vector<double> root_host;       // the same, (lo, hi) per variable
     std::vector<double> criticals;       // from the last sid_prove
 };
 
@@ -273,6 +274,103 @@ __global__ void k_store_criticals(const double2* box, std::uint64_t stride, cons
     }
 }
 
+/// Precision form, per-parent pass: each parent's box rounded outward to float, and for the split
+/// variable RD(lb), RU(lb), RD(w), RU(w), RU(ub) with w = (ub - lb) / nsub computed in double exactly as
+/// split_child does. One thread per parent, so the double work is paid once per parent, not per child.
+__global__ void k_parent_f32(const double2* in_box, std::uint64_t in_stride, std::uint64_t item0, std::uint64_t n_items,
+                             int nargs, int var, int nsub, float2* pbox, float4* psplit, std::uint64_t pstride) {
+    const std::uint64_t j = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(j >= n_items) return;
+    for(int v = 0; v < nargs; ++v) {
+        const double2 b = in_box[std::uint64_t(v) * in_stride + item0 + j];
+        pbox[std::uint64_t(v) * pstride + j] = make_float2(__double2float_rd(b.x), __double2float_ru(b.y));
+        if(v == var) {
+            const double w = __ddiv_rd(__dsub_rd(b.y, b.x), double(nsub));
+            psplit[j] = make_float4(__double2float_rd(w), __double2float_ru(b.x), __double2float_ru(w), 0.0f);
+        }
+    }
+}
+
+/// Quantization of the batch ordering: cell of a corner coordinate x = (float(x) - off) * scale.
+struct MortonQuant {
+    float off[16];
+    float scale[16];     // 2^bits / (root range), so cells are 0 .. 2^bits - 1
+};
+
+constexpr int kTileLog = 18;         // ordering tile: 2^18 consecutive cuboids (~12 MB of boxes, L2-resident)
+constexpr int kTileKeyBits = 16;     // Morton key bits within a tile (bits per variable = 16 / nargs, >= 1)
+
+/// Batch ordering (sid_eval_batch*), step 1: bucket of each cuboid = (its tile, Morton code of its lower
+/// corner quantized over the lemma's root box; in float: only the cell matters), and the histogram.
+__global__ void k_order_keys(const double* lo, std::uint64_t n, int nargs, const MortonQuant qp, int bits,
+                             std::uint32_t* key, std::uint32_t* count) {
+    const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    std::uint32_t k = 0;
+    std::uint32_t q[16];
+    const float top = float((1u << bits) - 1u);
+    for(int v = 0; v < nargs; ++v) {
+        float u = (__double2float_rn(lo[std::uint64_t(v) * n + i]) - qp.off[v]) * qp.scale[v];
+        u = u > 0.0f ? (u < top ? u : top) : 0.0f;   // NaN and out-of-box corners are clamped
+        q[v] = std::uint32_t(u);
+    }
+    for(int b = bits - 1; b >= 0; --b) {
+        for(int v = nargs - 1; v >= 0; --v) k = (k << 1) | ((q[v] >> b) & 1u);
+    }
+    k |= std::uint32_t(i >> kTileLog) << kTileKeyBits;
+    key[i] = k;
+    atomicAdd(&count[k], 1u);
+}
+
+/// Exclusive scan of `x` (n <= 2^24 entries) in place, in three launches: per-block scans of 4096
+/// entries with block totals, a one-block scan of the totals, and the addition of block offsets.
+__global__ void __launch_bounds__(1024) k_scan_blocks(std::uint32_t* x, std::uint64_t n, std::uint32_t* totals) {
+    __shared__ std::uint32_t warp_sums[32];
+    const std::uint64_t base = std::uint64_t(blockIdx.x) * 4096 + std::uint64_t(threadIdx.x) * 4;
+    std::uint32_t v[4];
+    std::uint32_t sum = 0;
+    for(int k = 0; k < 4; ++k) {
+        v[k] = base + k < n ? x[base + k] : 0u;
+        sum += v[k];
+    }
+    std::uint32_t incl = sum;
+    for(int d = 1; d < 32; d <<= 1) {
+        const std::uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+        if(int(threadIdx.x & 31u) >= d) incl += y;
+    }
+    if((threadIdx.x & 31u) == 31u) warp_sums[threadIdx.x >> 5] = incl;
+    __syncthreads();
+    if(threadIdx.x < 32) {
+        std::uint32_t w = warp_sums[threadIdx.x];
+        for(int d = 1; d < 32; d <<= 1) {
+            const std::uint32_t y = __shfl_up_sync(0xffffffffu, w, d);
+            if(int(threadIdx.x) >= d) w += y;
+        }
+        warp_sums[threadIdx.x] = w;
+    }
+    __syncthreads();
+    const std::uint32_t warp_off = (threadIdx.x >> 5) ? warp_sums[(threadIdx.x >> 5) - 1] : 0u;
+    std::uint32_t run = warp_off + incl - sum;
+    for(int k = 0; k < 4; ++k) {
+        if(base + k < n) x[base + k] = run;
+        run += v[k];
+    }
+    if(threadIdx.x == blockDim.x - 1) totals[blockIdx.x] = warp_off + incl;
+}
+
+__global__ void k_scan_add(std::uint32_t* x, std::uint64_t n, const std::uint32_t* offsets) {
+    const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(i < n) x[i] += offsets[i / 4096];
+}
+
+/// Step 3: place each cuboid at the next free position of its bucket. The order within a bucket is
+/// immaterial (every cuboid's result is independent of its neighbours), and a cuboid never leaves its tile.
+__global__ void k_order_scatter(const std::uint32_t* key, std::uint64_t n, std::uint32_t* offset, std::uint32_t* order) {
+    const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    order[atomicAdd(&offset[key[i]], 1u)] = std::uint32_t(i);
+}
+
 struct GatherEntry {
     std::uint32_t slot;
     std::uint32_t pad;
@@ -322,6 +420,8 @@ struct Lane {
     BoxList step, fin, nonfin;
     std::vector<std::unique_ptr<BoxList>> stat_levels, dyn_levels;
     DevBuf<std::uint32_t> esc;
+    DevBuf<float2> pbox;                  // precision form: per-parent float boxes of one chunk
+    DevBuf<float4> psplit;
     DevBuf<GatherEntry> gather;
     std::vector<GatherEntry> gather_host;
     long long grown_bytes = 0;             // device bytes request queues grew by since the last take_grown_bytes
@@ -507,7 +607,8 @@ struct Lane {
             cuda_check(lem->k->level(mode, a, st), "level kernel launch");
             return;
         }
-        // precision form: float pass over a chunk of children, then double pass over its escalation list
+        // precision form: per-parent float data, float pass over a chunk of children, then double pass over
+        // the chunk's escalation list
         for(std::uint64_t cb = 0; cb < total; cb += kEscChunk) {
             LevelArgs a = a0;
             a.count_cuboids = false;
@@ -515,6 +616,18 @@ struct Lane {
             a.n_child = std::min(kEscChunk, total - cb);
             a.esc = esc.p;
             a.esc_count = counters.p + 3;
+            const std::uint64_t nsub = std::uint64_t(a.nsub);
+            const std::uint64_t first = cb / nsub, n_items = (cb + a.n_child - 1) / nsub - first + 1;
+            pbox.reserve(std::size_t(n) * n_items);
+            psplit.reserve(n_items);
+            k_parent_f32<<<unsigned((n_items + 127) / 128), 128, 0, st>>>(a.in_box, a.in_stride, a.in_begin + first,
+                                                                          n_items, n, a.var, a.nsub, pbox.p, psplit.p,
+                                                                          n_items);
+            cuda_check(cudaGetLastError(), "parent pass launch");
+            a.pbox = pbox.p;
+            a.psplit = psplit.p;
+            a.pstride = n_items;
+            a.pitem_begin = first;
             cuda_check(cudaMemsetAsync(a.esc_count, 0, sizeof(unsigned long long), st), "reset escalation count");
             cuda_check(lem->k->filter_f32(a, st), "float pass launch");
             const std::uint64_t want = (a.n_child + 127) / 128;
@@ -740,6 +853,9 @@ struct sid_engine {
     std::map<int, std::unique_ptr<sid::Lane>> prove_lanes;   // lanes of sid_prove, one per lemma
     DevBuf<double> batch_in_lo, batch_in_hi, batch_out_lo, batch_out_hi;
     DevBuf<std::int8_t> batch_verdict;
+    DevBuf<std::uint32_t> batch_key, batch_order, batch_count, batch_totals;
+    bool batch_profile = false;
+    std::vector<cudaEvent_t> batch_events;   // four per profiled call: start, ordered, evaluated, scattered
 };
 
 namespace {
@@ -753,6 +869,60 @@ Lemma* get_lemma(sid_engine* e, int id) {
 }
 
 void set_device(sid_engine* e) { cuda_check(cudaSetDevice(e->device), "cudaSetDevice"); }
+
+void profile_mark(sid_engine* eng, cudaStream_t s) {
+    if(!eng->batch_profile) return;
+    cudaEvent_t ev;
+    cuda_check(cudaEventCreate(&ev), "profile event");
+    eng->batch_events.push_back(ev);
+    cuda_check(cudaEventRecord(ev, s), "profile event record");
+}
+
+void profile_clear(sid_engine* eng) {
+    for(cudaEvent_t ev : eng->batch_events) cudaEventDestroy(ev);
+    eng->batch_events.clear();
+}
+
+
+/// Evaluate a batch of n cuboids (SoA, device) in the order (tile of 2^18 cuboids, Morton code of the
+/// lower corner); results go to the cuboids' own positions. Asynchronous on `s`.
+void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const double* hi, std::uint64_t n, double* out_lo,
+                        double* out_hi, std::int8_t* verdict, cudaStream_t s) {
+    const int nargs = lem->ir.nargs;
+    profile_mark(eng, s);
+    const std::uint32_t* order = nullptr;
+    const std::uint64_t tiles = (n + (std::uint64_t(1) << kTileLog) - 1) >> kTileLog;
+    const std::uint64_t buckets = tiles << kTileKeyBits;
+    const std::uint64_t blocks = (buckets + 4095) / 4096;
+    if(n >= 4096 && n <= 0xffffffffull && nargs <= 16 && blocks <= 4096) {
+        const int bits = std::max(1, kTileKeyBits / std::max(nargs, 1));
+        MortonQuant qp{};
+        for(int v = 0; v < nargs; ++v) {
+            const double rl = lem->root_host[std::size_t(2 * v)], rh = lem->root_host[std::size_t(2 * v + 1)];
+            const double range = rh - rl;
+            qp.off[v] = float(rl);
+            qp.scale[v] = range > 0.0 && range < 1e300 ? float(double(1u << bits) / range) : 0.0f;
+        }
+        eng->batch_key.reserve(std::size_t(n));
+        eng->batch_order.reserve(std::size_t(n));
+        eng->batch_count.reserve(std::size_t(buckets));
+        eng->batch_totals.reserve(std::size_t(blocks) + 1);
+        cuda_check(cudaMemsetAsync(eng->batch_count.p, 0, buckets * sizeof(std::uint32_t), s), "order histogram reset");
+        const unsigned g = unsigned((n + 255) / 256);
+        k_order_keys<<<g, 256, 0, s>>>(lo, n, nargs, qp, bits, eng->batch_key.p, eng->batch_count.p);
+        k_scan_blocks<<<unsigned(blocks), 1024, 0, s>>>(eng->batch_count.p, buckets, eng->batch_totals.p);
+        k_scan_blocks<<<1, 1024, 0, s>>>(eng->batch_totals.p, blocks, eng->batch_totals.p + blocks);
+        k_scan_add<<<unsigned((buckets + 255) / 256), 256, 0, s>>>(eng->batch_count.p, buckets, eng->batch_totals.p);
+        k_order_scatter<<<g, 256, 0, s>>>(eng->batch_key.p, n, eng->batch_count.p, eng->batch_order.p);
+        cuda_check(cudaGetLastError(), "batch ordering");
+        order = eng->batch_order.p;
+    }
+    profile_mark(eng, s);
+    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order};
+    cuda_check(lem->k->eval_batch(a, s), "eval batch");
+    profile_mark(eng, s);
+    profile_mark(eng, s);
+}
 
 void check_precision(int precision) {
     if(precision != SID_PRECISION_PLAIN && precision != SID_PRECISION_FP32_ESCALATE) {
@@ -1033,6 +1203,7 @@ void sid_engine_destroy(sid_engine* engine) {
         cudaStream_t s = engine->stream;
         engine->prove_lanes.clear();
         engine->lemmas.clear();
+        profile_clear(engine);
         owner.reset();
         if(s) cudaStreamDestroy(s);
     }
@@ -1059,6 +1230,9 @@ int sid_lemma_register(sid_engine* engine, const char* ir, size_t ir_len, int* l
         set_device(engine);
         lem->root.reserve(std::size_t(lem->ir.nargs));
         cuda_check(lem->k->root_box(lem->root.p, engine->stream), "root box");
+        lem->root_host.assign(std::size_t(2 * lem->ir.nargs), 0.0);
+        cuda_check(cudaMemcpyAsync(lem->root_host.data(), lem->root.p, sizeof(double2) * std::size_t(lem->ir.nargs),
+                                   cudaMemcpyDeviceToHost, engine->stream), "root box copy");
         cuda_check(cudaStreamSynchronize(engine->stream), "root box sync");
         engine->lemmas.push_back(std::move(lem));
         *lemma_id = int(engine->lemmas.size() - 1);
@@ -1118,8 +1292,8 @@ int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, co
         Lemma* l = get_lemma(engine, lemma_id);
         if(l->k->is_f32) fail(SID_ERR_UNSUPPORTED, "batch evaluation supports double lemmas");
         set_device(engine);
-        BatchArgs a{lo, hi, out_lo, out_hi, verdict, n};
-        cuda_check(l->k->eval_batch(a, static_cast<cudaStream_t>(stream)), "eval batch");
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        eval_batch_ordered(engine, l, lo, hi, n, out_lo, out_hi, verdict, s);
     });
 }
 
@@ -1138,13 +1312,43 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
         cudaStream_t s = engine->stream;
         cuda_check(cudaMemcpyAsync(engine->batch_in_lo.p, lo, cnt * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
         cuda_check(cudaMemcpyAsync(engine->batch_in_hi.p, hi, cnt * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
-        BatchArgs a{engine->batch_in_lo.p, engine->batch_in_hi.p, engine->batch_out_lo.p, engine->batch_out_hi.p,
-                    engine->batch_verdict.p, n};
-        cuda_check(l->k->eval_batch(a, s), "eval batch");
+        eval_batch_ordered(engine, l, engine->batch_in_lo.p, engine->batch_in_hi.p, n, engine->batch_out_lo.p,
+                           engine->batch_out_hi.p, engine->batch_verdict.p, s);
         cuda_check(cudaMemcpyAsync(out_lo, engine->batch_out_lo.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaMemcpyAsync(out_hi, engine->batch_out_hi.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaMemcpyAsync(verdict, engine->batch_verdict.p, std::size_t(n), cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaStreamSynchronize(s), "eval batch sync");
+    });
+}
+
+int sid_eval_batch_profile(sid_engine* engine, int enable) {
+    return guarded([&] {
+        if(!engine) fail(SID_ERR_INVALID, "null engine");
+        set_device(engine);
+        engine->batch_profile = enable != 0;
+        if(!enable) profile_clear(engine);
+    });
+}
+
+int sid_eval_batch_profile_read(sid_engine* engine, uint64_t* calls, double* order_ms, double* eval_ms) {
+    return guarded([&] {
+        if(!engine || !calls || !order_ms || !eval_ms) fail(SID_ERR_INVALID, "null argument");
+        set_device(engine);
+        *calls = 0;
+        *order_ms = 0;
+        *eval_ms = 0;
+        const std::size_t k = engine->batch_events.size() / 4 * 4;
+        for(std::size_t i = 0; i < k; i += 4) {
+            cuda_check(cudaEventSynchronize(engine->batch_events[i + 3]), "profile event wait");
+            float a = 0, b = 0, c = 0;
+            cuda_check(cudaEventElapsedTime(&a, engine->batch_events[i], engine->batch_events[i + 1]), "profile time");
+            cuda_check(cudaEventElapsedTime(&b, engine->batch_events[i + 1], engine->batch_events[i + 2]), "profile time");
+            cuda_check(cudaEventElapsedTime(&c, engine->batch_events[i + 2], engine->batch_events[i + 3]), "profile time");
+            *order_ms += a + c;
+            *eval_ms += b;
+            *calls += 1;
+        }
+        profile_clear(engine);
     });
 }
 

@@ -205,6 +205,10 @@ struct LevelArgs {
     std::uint64_t child_begin, n_child;
     std::uint32_t* esc;
     unsigned long long* esc_count;
+    // per-parent float data of the chunk (k_parent_f32): parents from item offset pitem_begin on
+    const float2* pbox;               // pbox[v*pstride + j]; for the split variable (RD(lb), RU(ub))
+    const float4* psplit;             // (RD(w), RU(lb), RU(w), 0) with w the double split width
+    std::uint64_t pstride, pitem_begin;
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -358,11 +362,20 @@ template<class L, class T, int MODE> __global__ void __launch_bounds__(128) k_le
     level_child<L, T, MODE>(a, a.in_begin + t / std::uint64_t(a.nsub), int(t % std::uint64_t(a.nsub)), active);
 }
 
+/// Float box of child c of a parent from its k_parent_f32 data: it contains the double child box of
+/// split_child. lo = RD(RD(lb) + RD(c*RD(w))) <= RD(lb + RD(c*w)); hi = RU(RU(lb) + RU((c+1)*RU(w))) >=
+/// lb + (c+1)*w >= the double split point; the last child ends at RU(ub). (The oracle's precision form
+/// builds the same float box.)
+__device__ __forceinline__ void split_child_f32(float lb_lo, float ub_hi, float4 sp, int n, int c, float& lo, float& hi) {
+    lo = __fadd_rd(lb_lo, __fmul_rd(float(c), sp.x));
+    hi = (c + 1 >= n) ? ub_hi : __fadd_ru(sp.y, __fmul_ru(float(c + 1), sp.z));
+}
+
 /// Precision form, first pass: children [child_begin, child_begin + n_child) of the launch's items
-/// (child id = item offset * nsub + child) are split in double exactly as in the plain form, rounded
-/// outward to float, and propagated and tested in float. A child refuted in float is a leaf (interval
-/// arithmetic in float is as sound as in double); every other child id goes to the escalation list,
-/// whose children are then evaluated in double by k_level_esc, with double results used throughout.
+/// (child id = item offset * nsub + child) are propagated and tested in float on a float box that
+/// contains the double child box. A child refuted in float is a leaf (interval arithmetic in float is as
+/// sound as in double); every other child id goes to the escalation list, whose children are then
+/// evaluated in double by k_level_esc, with double results used throughout.
 template<class L> __global__ void __launch_bounds__(128) k_filter_f32(const LevelArgs a) {
     constexpr int N = L::NARGS;
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -370,13 +383,14 @@ template<class L> __global__ void __launch_bounds__(128) k_filter_f32(const Leve
     const unsigned active = __activemask();
     const std::uint64_t id = a.child_begin + t;
     const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
+    const std::uint64_t j = id / std::uint64_t(a.nsub) - a.pitem_begin;
     const int c = int(id % std::uint64_t(a.nsub));
     Iv<float> box[N];
     #pragma unroll
     for(int v = 0; v < N; ++v) {
-        double2 b = a.in_box[std::uint64_t(v) * a.in_stride + item];
-        if(v == a.var) split_child(b.x, b.y, a.nsub, c, b.x, b.y);
-        box[v] = {__double2float_rd(b.x), __double2float_ru(b.y), false};
+        const float2 f = a.pbox[std::uint64_t(v) * a.pstride + j];
+        box[v] = {f.x, f.y, false};
+        if(v == a.var) split_child_f32(f.x, f.y, a.psplit[j], a.nsub, c, box[v].lo, box[v].hi);
     }
     bool ok = !propagate<L, float>(a.var, box, a.it_limit, a.rec_limit);
     if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<float>(a.row_begin, a.row_end, box);
@@ -436,14 +450,19 @@ struct BatchArgs {
     double* out_lo; double* out_hi;
     std::int8_t* verdict;
     std::uint64_t n;
+    const std::uint32_t* order;   // thread t evaluates cuboid order[t] (nullptr: cuboid t)
 };
 
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
-/// (it_limit = nargs, rec_limit = 4) and test all constraints.
+/// (it_limit = nargs, rec_limit = 4) and test all constraints. Threads follow `order` when given (the
+/// host orders each tile of 2^18 cuboids by the Morton code of the cuboids' positions, so that a warp's
+/// cuboids take the same branches, sign cases and propagation orders, while the permuted accesses stay in
+/// an L2-sized window); results go to each cuboid's own position.
 template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(const BatchArgs a) {
     constexpr int N = L::NARGS;
-    const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if(i >= a.n) return;
+    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(t >= a.n) return;
+    const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
     Iv<T> box[N];
     #pragma unroll
     for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * a.n + i]), T(a.hi[std::uint64_t(v) * a.n + i]), false};

@@ -23,7 +23,7 @@ EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "si
             "sid_lemma_register", "sid_lemma_info", "sid_lemma_root_box", "sid_prove", "sid_fetch_criticals",
             "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc", "sid_server_opts_default",
             "sid_server_create", "sid_server_destroy", "sid_submit", "sid_request_poll", "sid_request_wait",
-            "sid_request_criticals", "sid_request_release"]
+            "sid_request_criticals", "sid_request_release", "sid_eval_batch_profile", "sid_eval_batch_profile_read"]
 
 PRECISION_PLAIN, PRECISION_FP32 = 0, 1
 REQ_PENDING, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
@@ -111,6 +111,9 @@ def load(path=LIB_PATH):
     L.sid_request_criticals.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                                         ctypes.POINTER(ctypes.c_uint64)]
     L.sid_request_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+    L.sid_eval_batch_profile.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.sid_eval_batch_profile_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     _lib = L
     return L
 
@@ -215,6 +218,16 @@ class Engine:
         _check(self.L.sid_eval_batch_device(self.h, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr,
                                             verdict_ptr, stream))
 
+
+    def batch_profile(self, enable):
+        """Record CUDA events around the ordering and evaluation kernels of the following batch calls."""
+        _check(self.L.sid_eval_batch_profile(self.h, 1 if enable else 0))
+
+    def batch_profile_read(self):
+        """(calls, ordering ms, evaluation ms) summed over the recorded batch calls; clears the record."""
+        calls, a, b = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double()
+        _check(self.L.sid_eval_batch_profile_read(self.h, ctypes.byref(calls), ctypes.byref(a), ctypes.byref(b)))
+        return calls.value, a.value, b.value
 
     def leaf_hull_noalloc(self, lemma_id, boxes_ptr, n, hulls_ptr, nonempty_ptr, leaves_ptr, stream=0):
         """Allocation-free leaf hulls on caller device buffers (see sid_leaf_hull_noalloc in sid.h)."""
