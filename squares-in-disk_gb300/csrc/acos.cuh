@@ -15,19 +15,21 @@
 //   x < -1/2   :  acos(x) = pi - 2 asin(sqrt((1+x)/2)),
 // with asin(t) = t * sum C_k t^(2k) (t <= 1/2, Horner, exact rational coefficients rounded to the
 // format) and sqrt(w) = w * y where y = 1/sqrt(w) is refined by Newton steps
-// y <- y (3 - w y^2) / 2 from a double start value (the argument is first scaled by an even power
-// of two into [1/4, 1)). (1-x)/2 and (1+x)/2 are exact in double.
+// y <- y (3 - w y^2) / 2 from a float start value (the argument is first scaled by an even power
+// of two into [1/4, 1)). (1-x)/2 and (1+x)/2 are exact in the format. Apart from that float start
+// (rsqrtf) everything is integer arithmetic: GB300's FP64 pipe is not used at all.
 //
 // Error bound (all products truncated, each costs at most one unit): the series value is within
 // 4.1 + 1.4 e_t units of the exact sum for an argument with error e_t, asin within 3.1 + 1.8 e_t,
-// the square root within 3.5 units, so the result is within 19 units of acos(x); kErrUnits = 64
+// the square root within 3.5 units (the Newton steps from a start good to 2^-12 reach far below one
+// unit), so the result is within 19 units of acos(x); kErrUnits = 64
 // is used. The result is rounded to the target precision from the enclosure
 // [R - 64 units, R + 64 units]: when both ends round down to the same floating-point number d,
 // acos(x) lies strictly between d and its successor (acos(x) is transcendental for every
 // floating-point x except 1, Lindemann-Weierstrass), so d is the downward and its successor the
-// upward rounding. Two limbs (125 fractional bits) decide all but a vanishing fraction of the
-// arguments; the rest are evaluated again with four limbs (253 fractional bits), which is more
-// precision than any double argument needs. If even that left the rounding undecided, the result
+// upward rounding. For float results one limb (61 fractional bits) decides all but a vanishing
+// fraction of the arguments, for double results two limbs (125 bits); the rest are evaluated again
+// with more limbs, up to four (253 fractional bits), which is more precision than any argument needs. If even that left the rounding undecided, the result
 // would be the outward enclosure itself (still a valid bound).
 //
 // The same source compiles for the host (tests/acos_check.cpp checks it against 300-bit mpmath).
@@ -115,15 +117,6 @@ SID_ACOS_HD inline int clz64(std::uint64_t v) {
     return __clzll(static_cast<long long>(v));
 #else
     return __builtin_clzll(v);
-#endif
-}
-
-// 1/sqrt(m) for m in [1/4, 1), correctly rounded operations (any start value within 2^-40 works).
-SID_ACOS_HD inline double rsqrt_start(double m) {
-#if defined(__CUDA_ARCH__)
-    return __drcp_rn(__dsqrt_rn(m));
-#else
-    return 1.0 / __builtin_sqrt(m);
 #endif
 }
 
@@ -243,9 +236,9 @@ SID_ACOS_UNROLL
     return r;
 }
 
-// A non-negative double below 8, truncated to the format (exact when its last bit is >= 1 unit).
-template<int NL> SID_ACOS_HD inline Fx<NL> fx_from_double(double x) {
-    std::uint64_t b = bits_of(x);
+// A non-negative double (given by its bits) below 8, truncated to the format (exact when its last bit
+// is >= 1 unit).
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_from_bits(std::uint64_t b) {
     int be = static_cast<int>((b >> 52) & 0x7ff);
     Fx<NL> r = fx_zero<NL>();
     if(be == 0) return r;   // zero or subnormal: below one unit
@@ -260,9 +253,71 @@ SID_ACOS_UNROLL
     return r;
 }
 
+// A positive normal float (given by its bits) below 8, in the format (exact).
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_from_float_bits(std::uint32_t b) {
+    const std::uint64_t m = std::uint64_t((b & 0x7fffffu) | 0x800000u);
+    const int s = int((b >> 23) & 0xffu) - 150 + (64 * NL - 3);   // bit position of the last mantissa bit
+    Fx<NL> r = fx_zero<NL>();
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) {
+        int d = s - 64 * i;
+        if(d >= 0) r.w[i] = d < 64 ? m << d : 0;
+        else r.w[i] = d > -64 ? m >> -d : 0;
+    }
+    return r;
+}
+
+// Index of the highest set bit (-1 for zero).
+template<int NL> SID_ACOS_HD inline int fx_top_bit(const Fx<NL>& v) {
+    int p = -1;
+SID_ACOS_UNROLL
+    for(int i = NL - 1; i >= 0; --i) {
+        if(p < 0 && v.w[i] != 0) p = 64 * i + 63 - clz64(v.w[i]);
+    }
+    return p;
+}
+
+// Left shift by s bits, 0 <= s < 64 NL (limbs selected with compile-time indices only).
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_shl(const Fx<NL>& a, int s) {
+    const int q = s >> 6, b = s & 63;
+    Fx<NL> r;
+SID_ACOS_UNROLL
+    for(int i = 0; i < NL; ++i) {
+        std::uint64_t hi = 0, lo = 0;
+SID_ACOS_UNROLL
+        for(int k = 0; k < NL; ++k) {
+            if(k == i - q) hi = a.w[k];
+            if(k == i - q - 1) lo = a.w[k];
+        }
+        r.w[i] = (hi << b) | (b ? lo >> (64 - b) : 0);
+    }
+    return r;
+}
+
+SID_ACOS_HD inline float rsqrt_f32(float m) {
+#if defined(__CUDA_ARCH__)
+    return rsqrtf(m);
+#else
+    return 1.0f / __builtin_sqrtf(m);
+#endif
+}
+
+SID_ACOS_HD inline std::uint32_t float_bits(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(x);
+#else
+    std::uint32_t b;
+    std::memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+
+// Series length (64 NL - 3 fractional bits need (1/4)^k below one unit) and Newton steps of the reciprocal
+// square root (from a float start good to 2^-12 or better; each step squares the relative error).
 template<int NL> struct Terms;
-template<> struct Terms<2> { static constexpr int count = 64; static constexpr int newton = 2; };
-template<> struct Terms<4> { static constexpr int count = 128; static constexpr int newton = 3; };
+template<> struct Terms<1> { static constexpr int count = 32; static constexpr int newton = 3; };
+template<> struct Terms<2> { static constexpr int count = 64; static constexpr int newton = 4; };
+template<> struct Terms<4> { static constexpr int count = 128; static constexpr int newton = 5; };
 
 // asin(t) for t <= 1/2 (plus rounding slack).
 template<int NL> SID_ACOS_HD inline Fx<NL> fx_asin(const Fx<NL>& t) {
@@ -272,14 +327,16 @@ template<int NL> SID_ACOS_HD inline Fx<NL> fx_asin(const Fx<NL>& t) {
     return fx_mul(t, s);
 }
 
-// sqrt(w) for a double w in [0, 1/4).
-template<int NL> SID_ACOS_HD inline Fx<NL> fx_sqrt_small(double w) {
-    if(w == 0.0) return fx_zero<NL>();
-    int k = static_cast<int>((bits_of(w) >> 52) & 0x7ff) - 1023;   // w = f 2^k, f in [1, 2), k <= -3
-    int e = (k & 1) ? (-1 - k) / 2 : (-2 - k) / 2;                  // m = w 4^e in [1/4, 1), 1 <= e <= 26
-    double m = w * double_of(static_cast<std::uint64_t>(1023 + 2 * e) << 52);
-    Fx<NL> mm = fx_from_double<NL>(m);
-    Fx<NL> y = fx_from_double<NL>(rsqrt_start(m));
+// sqrt(w) for an exact w in [0, 1/4): w = m 4^-e with m in [1/4, 1), y = 1/sqrt(m) by Newton steps
+// y <- y (3 - m y^2) / 2 from a float start, sqrt(w) = (m y) 2^-e.
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_sqrt_small(const Fx<NL>& w) {
+    constexpr int F = 64 * NL - 3;
+    const int p = fx_top_bit(w);
+    if(p < 0) return fx_zero<NL>();
+    const int e = (F - 1 - p) >> 1;                       // 1 <= e: the top bit of m is F-1 or F-2
+    const Fx<NL> mm = fx_shl(w, 2 * e);
+    const float mf = float(std::uint32_t(mm.w[NL - 1] >> 37)) * (1.0f / 16777216.0f);   // m to 24 bits
+    Fx<NL> y = fx_from_float_bits<NL>(float_bits(rsqrt_f32(mf)));
     const Fx<NL> three = fx_int<NL>(3);
 SID_ACOS_UNROLL
     for(int it = 0; it < Terms<NL>::newton; ++it) {
@@ -289,27 +346,24 @@ SID_ACOS_UNROLL
     return fx_shr(fx_mul(mm, y), e);
 }
 
-// acos(x) for -1 <= x < 1, within 19 units.
-template<int NL> SID_ACOS_HD inline Fx<NL> fx_acos(double x) {
-    double ax = double_of(bits_of(x) & ~(std::uint64_t(1) << 63));
-    bool neg = (bits_of(x) >> 63) != 0;
-    if(ax <= 0.5) {
-        Fx<NL> a = fx_asin(fx_from_double<NL>(ax));
+// acos(x) for -1 <= x < 1 (x given by its double bits), within 19 units; integer arithmetic only.
+template<int NL> SID_ACOS_HD inline Fx<NL> fx_acos(std::uint64_t xb) {
+    const std::uint64_t ab = xb & ~(std::uint64_t(1) << 63);
+    const bool neg = (xb >> 63) != 0;
+    if(ab <= 0x3fe0000000000000ull) {                      // |x| <= 1/2
+        Fx<NL> a = fx_asin(fx_from_bits<NL>(ab));
         Fx<NL> h = fx_row<NL>(kRowPiHalf);
         return neg ? fx_add(h, a) : fx_sub(h, a);
     }
-    Fx<NL> a2 = fx_shl1(fx_asin(fx_sqrt_small<NL>((1.0 - ax) * 0.5)));
+    const Fx<NL> w = fx_shr(fx_sub(fx_int<NL>(1), fx_from_bits<NL>(ab)), 1);   // (1 - |x|) / 2, exact
+    Fx<NL> a2 = fx_shl1(fx_asin(fx_sqrt_small(w)));
     return neg ? fx_sub(fx_row<NL>(kRowPi), a2) : a2;
 }
 
 // The largest floating-point number with `digits` significant bits that is <= v (v > 0), as
 // (significand, exponent of its leading bit relative to the format's units).
 template<int NL> SID_ACOS_HD inline void fx_floor_fp(const Fx<NL>& v, int digits, std::uint64_t& mant, int& lead) {
-    int p = -1;
-SID_ACOS_UNROLL
-    for(int i = NL - 1; i >= 0; --i) {
-        if(p < 0 && v.w[i] != 0) p = 64 * i + 63 - clz64(v.w[i]);
-    }
+    const int p = fx_top_bit(v);
     int q = p - digits + 1;   // position of the last kept bit (>= 0: values here are >= 2^-31)
     std::uint64_t win = 0;
 SID_ACOS_UNROLL
@@ -324,9 +378,9 @@ SID_ACOS_UNROLL
 
 // Downward rounding of acos(x) for -1 <= x < 1 at `digits` bits; false if NL limbs cannot decide
 // it (then mant/lead describe the floor of the enclosure's lower end and mant_hi/lead_hi its upper).
-template<int NL> SID_ACOS_HD inline bool acos_floor(double x, int digits, std::uint64_t& mant, int& lead,
+template<int NL> SID_ACOS_HD inline bool acos_floor(std::uint64_t xb, int digits, std::uint64_t& mant, int& lead,
                                                     std::uint64_t& mant_hi, int& lead_hi) {
-    Fx<NL> r = fx_acos<NL>(x);
+    Fx<NL> r = fx_acos<NL>(xb);
     Fx<NL> err = fx_units<NL>(kErrUnits);
     Fx<NL> lo = fx_less(err, r) ? fx_sub(r, err) : fx_units<NL>(1);
     Fx<NL> hi = fx_add(r, err);
@@ -335,35 +389,51 @@ template<int NL> SID_ACOS_HD inline bool acos_floor(double x, int digits, std::u
     return mant == mant_hi && lead == lead_hi;
 }
 
-// acos(x) rounded down (up = false) or up (up = true) to double (digits 53) or float (digits 24),
-// as bit patterns. NaN and arguments outside [-1, 1] give NaN; acos(1) = +0.
-template<int DIGITS> SID_ACOS_HD SID_ACOS_NOINLINE std::uint64_t acos_rounded_bits(double x, bool up) {
-    constexpr int kFrac2 = 64 * 2 - 3, kFrac4 = 64 * 4 - 3;
+// acos(x) rounded down (up = false) or up (up = true) to double (digits 53) or float (digits 24), as bit
+// patterns, for x given by its double bits. NaN and arguments outside [-1, 1] give NaN; acos(1) = +0.
+// Float results try one limb first, double results two; undecided roundings retry with more limbs.
+template<int DIGITS> SID_ACOS_HD SID_ACOS_NOINLINE std::uint64_t acos_rounded_bits(std::uint64_t xb, bool up) {
     constexpr int kBias = DIGITS == 53 ? 1023 : 127;
     constexpr std::uint64_t kNaN = DIGITS == 53 ? 0x7ff8000000000000ull : 0x7fc00000ull;
-    if(!(x >= -1.0 && x <= 1.0)) return kNaN;
-    if(x == 1.0) return 0;
-    std::uint64_t mant, mant_hi;
-    int lead, lead_hi, frac = kFrac2;
-    if(!acos_floor<2>(x, DIGITS, mant, lead, mant_hi, lead_hi)) {
-        frac = kFrac4;
-        if(!acos_floor<4>(x, DIGITS, mant, lead, mant_hi, lead_hi) && up) {
-            mant = mant_hi;   // undecided even with four limbs: outward enclosure
-            lead = lead_hi;
-        }
+    const std::uint64_t ab = xb & ~(std::uint64_t(1) << 63);
+    if(ab > 0x3ff0000000000000ull) return kNaN;             // |x| > 1 or NaN
+    if(xb == 0x3ff0000000000000ull) return 0;              // acos(1) = +0
+    std::uint64_t mant = 0, mant_hi = 0;
+    int lead = 0, lead_hi = 0, frac = 64 * 4 - 3;
+    bool done = false;
+    if(DIGITS == 24 && acos_floor<1>(xb, DIGITS, mant, lead, mant_hi, lead_hi)) {
+        frac = 64 - 3;
+        done = true;
+    }
+    if(!done && acos_floor<2>(xb, DIGITS, mant, lead, mant_hi, lead_hi)) {
+        frac = 64 * 2 - 3;
+        done = true;
+    }
+    if(!done && !acos_floor<4>(xb, DIGITS, mant, lead, mant_hi, lead_hi) && up) {
+        mant = mant_hi;   // undecided even with four limbs: outward enclosure
+        lead = lead_hi;
     }
     std::uint64_t b = (static_cast<std::uint64_t>(lead - frac + kBias) << (DIGITS - 1)) |
                       (mant & ((std::uint64_t(1) << (DIGITS - 1)) - 1));
     return up ? b + 1 : b;   // the successor of a positive number: next bit pattern
 }
 
-SID_ACOS_HD inline double acos_rd(double x) { return double_of(acos_rounded_bits<53>(x, false)); }
-SID_ACOS_HD inline double acos_ru(double x) { return double_of(acos_rounded_bits<53>(x, true)); }
+// Double bits of a float, by integer operations (float subnormals, far below one unit, map to zero).
+SID_ACOS_HD inline std::uint64_t f32_to_f64_bits(std::uint32_t f) {
+    const std::uint64_t sign = std::uint64_t(f >> 31) << 63;
+    const std::uint32_t e = (f >> 23) & 0xffu, m = f & 0x7fffffu;
+    if(e == 0xffu) return sign | (std::uint64_t(0x7ff) << 52) | (std::uint64_t(m) << 29);
+    if(e == 0) return sign;
+    return sign | (std::uint64_t(e - 127 + 1023) << 52) | (std::uint64_t(m) << 29);
+}
+
+SID_ACOS_HD inline double acos_rd(double x) { return double_of(acos_rounded_bits<53>(bits_of(x), false)); }
+SID_ACOS_HD inline double acos_ru(double x) { return double_of(acos_rounded_bits<53>(bits_of(x), true)); }
 SID_ACOS_HD inline float acos_rd(float x) {
-    return float_of(static_cast<std::uint32_t>(acos_rounded_bits<24>(x, false)));
+    return float_of(static_cast<std::uint32_t>(acos_rounded_bits<24>(f32_to_f64_bits(float_bits(x)), false)));
 }
 SID_ACOS_HD inline float acos_ru(float x) {
-    return float_of(static_cast<std::uint32_t>(acos_rounded_bits<24>(x, true)));
+    return float_of(static_cast<std::uint32_t>(acos_rounded_bits<24>(f32_to_f64_bits(float_bits(x)), true)));
 }
 
 } // namespace acos_cr

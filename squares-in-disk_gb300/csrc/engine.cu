@@ -302,15 +302,15 @@ constexpr int kTileKeyBits = 16;     // Morton key bits within a tile (bits per 
 
 /// Batch ordering (sid_eval_batch*), step 1: bucket of each cuboid = (its tile, Morton code of its lower
 /// corner quantized over the lemma's root box; in float: only the cell matters), and the histogram.
-__global__ void k_order_keys(const double* lo, std::uint64_t n, int nargs, const MortonQuant qp, int bits,
-                             std::uint32_t* key, std::uint32_t* count) {
+__global__ void k_order_keys(const double* lo, std::uint64_t n, std::uint64_t stride, int nargs, const MortonQuant qp,
+                             int bits, std::uint32_t* key, std::uint32_t* count) {
     const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if(i >= n) return;
     std::uint32_t k = 0;
     std::uint32_t q[16];
     const float top = float((1u << bits) - 1u);
     for(int v = 0; v < nargs; ++v) {
-        float u = (__double2float_rn(lo[std::uint64_t(v) * n + i]) - qp.off[v]) * qp.scale[v];
+        float u = (__double2float_rn(lo[std::uint64_t(v) * stride + i]) - qp.off[v]) * qp.scale[v];
         u = u > 0.0f ? (u < top ? u : top) : 0.0f;   // NaN and out-of-box corners are clamped
         q[v] = std::uint32_t(u);
     }
@@ -849,6 +849,7 @@ struct sid_engine {
     int device = 0;
     int sm_count = 1;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;   // sid_eval_batch's transfer streams
     std::vector<std::unique_ptr<Lemma>> lemmas;
     std::map<int, std::unique_ptr<sid::Lane>> prove_lanes;   // lanes of sid_prove, one per lemma
     DevBuf<double> batch_in_lo, batch_in_hi, batch_out_lo, batch_out_hi;
@@ -884,10 +885,11 @@ void profile_clear(sid_engine* eng) {
 }
 
 
-/// Evaluate a batch of n cuboids (SoA, device) in the order (tile of 2^18 cuboids, Morton code of the
-/// lower corner); results go to the cuboids' own positions. Asynchronous on `s`.
+/// Evaluate a batch of n cuboids (SoA, device, variables `stride` apart; 0: n) in the order (tile of 2^18
+/// cuboids, Morton code of the lower corner); results go to the cuboids' own positions. Asynchronous on `s`.
 void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const double* hi, std::uint64_t n, double* out_lo,
-                        double* out_hi, std::int8_t* verdict, cudaStream_t s) {
+                        double* out_hi, std::int8_t* verdict, cudaStream_t s, std::uint64_t stride = 0) {
+    if(stride == 0) stride = n;
     const int nargs = lem->ir.nargs;
     profile_mark(eng, s);
     const std::uint32_t* order = nullptr;
@@ -909,7 +911,7 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
         eng->batch_totals.reserve(std::size_t(blocks) + 1);
         cuda_check(cudaMemsetAsync(eng->batch_count.p, 0, buckets * sizeof(std::uint32_t), s), "order histogram reset");
         const unsigned g = unsigned((n + 255) / 256);
-        k_order_keys<<<g, 256, 0, s>>>(lo, n, nargs, qp, bits, eng->batch_key.p, eng->batch_count.p);
+        k_order_keys<<<g, 256, 0, s>>>(lo, n, stride, nargs, qp, bits, eng->batch_key.p, eng->batch_count.p);
         k_scan_blocks<<<unsigned(blocks), 1024, 0, s>>>(eng->batch_count.p, buckets, eng->batch_totals.p);
         k_scan_blocks<<<1, 1024, 0, s>>>(eng->batch_totals.p, blocks, eng->batch_totals.p + blocks);
         k_scan_add<<<unsigned((buckets + 255) / 256), 256, 0, s>>>(eng->batch_count.p, buckets, eng->batch_totals.p);
@@ -918,11 +920,13 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
         order = eng->batch_order.p;
     }
     profile_mark(eng, s);
-    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order};
+    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order, stride};
     cuda_check(lem->k->eval_batch(a, s), "eval batch");
     profile_mark(eng, s);
     profile_mark(eng, s);
 }
+
+constexpr std::uint64_t kBatchChunk = std::uint64_t(1) << 20;   // cuboids per transfer chunk of sid_eval_batch
 
 void check_precision(int precision) {
     if(precision != SID_PRECISION_PLAIN && precision != SID_PRECISION_FP32_ESCALATE) {
@@ -1190,6 +1194,8 @@ int sid_engine_create(int device, sid_engine** out) {
         set_device(e.get());
         cuda_check(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");
         cuda_check(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        cuda_check(cudaStreamCreateWithFlags(&e->copy_in, cudaStreamNonBlocking), "cudaStreamCreate");
+        cuda_check(cudaStreamCreateWithFlags(&e->copy_out, cudaStreamNonBlocking), "cudaStreamCreate");
         *out = e.release();
     });
 }
@@ -1201,11 +1207,14 @@ void sid_engine_destroy(sid_engine* engine) {
     {
         std::unique_ptr<sid_engine> owner(engine);
         cudaStream_t s = engine->stream;
+        cudaStream_t ci = engine->copy_in, co = engine->copy_out;
         engine->prove_lanes.clear();
         engine->lemmas.clear();
         profile_clear(engine);
         owner.reset();
         if(s) cudaStreamDestroy(s);
+        if(ci) cudaStreamDestroy(ci);
+        if(co) cudaStreamDestroy(co);
     }
 }
 
@@ -1303,21 +1312,62 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
         Lemma* l = get_lemma(engine, lemma_id);
         if(l->k->is_f32) fail(SID_ERR_UNSUPPORTED, "batch evaluation supports double lemmas");
         set_device(engine);
-        const std::size_t cnt = std::size_t(n) * std::size_t(l->ir.nargs);
+        const int nargs = l->ir.nargs;
+        const std::size_t cnt = std::size_t(n) * std::size_t(nargs);
         engine->batch_in_lo.reserve(cnt);
         engine->batch_in_hi.reserve(cnt);
         engine->batch_out_lo.reserve(cnt);
         engine->batch_out_hi.reserve(cnt);
         engine->batch_verdict.reserve(std::size_t(n));
-        cudaStream_t s = engine->stream;
-        cuda_check(cudaMemcpyAsync(engine->batch_in_lo.p, lo, cnt * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
-        cuda_check(cudaMemcpyAsync(engine->batch_in_hi.p, hi, cnt * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
-        eval_batch_ordered(engine, l, engine->batch_in_lo.p, engine->batch_in_hi.p, n, engine->batch_out_lo.p,
-                           engine->batch_out_hi.p, engine->batch_verdict.p, s);
-        cuda_check(cudaMemcpyAsync(out_lo, engine->batch_out_lo.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
-        cuda_check(cudaMemcpyAsync(out_hi, engine->batch_out_hi.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
-        cuda_check(cudaMemcpyAsync(verdict, engine->batch_verdict.p, std::size_t(n), cudaMemcpyDeviceToHost, s), "D2H");
-        cuda_check(cudaStreamSynchronize(s), "eval batch sync");
+        // Pipeline in chunks: copies in on copy_in, ordering + evaluation on the engine stream, copies out on
+        // copy_out, so transfers of one chunk overlap the evaluation of its neighbours.
+        const std::uint64_t chunk = kBatchChunk;
+        const std::uint64_t nchunks = (n + chunk - 1) / chunk;
+        std::vector<cudaEvent_t> evs;
+        auto event = [&]() {
+            cudaEvent_t e;
+            cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            evs.push_back(e);
+            return e;
+        };
+        try {
+            for(std::uint64_t c = 0; c < nchunks; ++c) {
+                const std::uint64_t c0 = c * chunk, len = std::min(chunk, n - c0);
+                for(int v = 0; v < nargs; ++v) {
+                    const std::uint64_t off = std::uint64_t(v) * n + c0;
+                    cuda_check(cudaMemcpyAsync(engine->batch_in_lo.p + off, lo + off, len * sizeof(double),
+                                               cudaMemcpyHostToDevice, engine->copy_in), "H2D");
+                    cuda_check(cudaMemcpyAsync(engine->batch_in_hi.p + off, hi + off, len * sizeof(double),
+                                               cudaMemcpyHostToDevice, engine->copy_in), "H2D");
+                }
+                cudaEvent_t in_done = event();
+                cuda_check(cudaEventRecord(in_done, engine->copy_in), "event record");
+                cuda_check(cudaStreamWaitEvent(engine->stream, in_done, 0), "stream wait");
+                eval_batch_ordered(engine, l, engine->batch_in_lo.p + c0, engine->batch_in_hi.p + c0, len,
+                                   engine->batch_out_lo.p + c0, engine->batch_out_hi.p + c0, engine->batch_verdict.p + c0,
+                                   engine->stream, n);
+                cudaEvent_t eval_done = event();
+                cuda_check(cudaEventRecord(eval_done, engine->stream), "event record");
+                cuda_check(cudaStreamWaitEvent(engine->copy_out, eval_done, 0), "stream wait");
+                for(int v = 0; v < nargs; ++v) {
+                    const std::uint64_t off = std::uint64_t(v) * n + c0;
+                    cuda_check(cudaMemcpyAsync(out_lo + off, engine->batch_out_lo.p + off, len * sizeof(double),
+                                               cudaMemcpyDeviceToHost, engine->copy_out), "D2H");
+                    cuda_check(cudaMemcpyAsync(out_hi + off, engine->batch_out_hi.p + off, len * sizeof(double),
+                                               cudaMemcpyDeviceToHost, engine->copy_out), "D2H");
+                }
+                cuda_check(cudaMemcpyAsync(verdict + c0, engine->batch_verdict.p + c0, std::size_t(len),
+                                           cudaMemcpyDeviceToHost, engine->copy_out), "D2H");
+            }
+            cuda_check(cudaStreamSynchronize(engine->copy_out), "eval batch sync");
+        } catch(...) {
+            cudaStreamSynchronize(engine->copy_in);
+            cudaStreamSynchronize(engine->stream);
+            cudaStreamSynchronize(engine->copy_out);
+            for(cudaEvent_t e : evs) cudaEventDestroy(e);
+            throw;
+        }
+        for(cudaEvent_t e : evs) cudaEventDestroy(e);
     });
 }
 

@@ -30,11 +30,13 @@ SID_ACOS_HD inline Out check_one(Case c) {
     o.dec2 = -1;
     o.dec4 = -1;
     o.rd4 = 0;
+    // the product's float path converts float arguments to double bits with integer operations
+    const std::uint64_t xb = c.is_float ? f32_to_f64_bits(float_bits(float(c.x))) : bits_of(c.x);
     if(c.x >= -1.0 && c.x < 1.0) {
         std::uint64_t m, mh;
         int l, lh;
-        o.dec2 = acos_floor<2>(c.x, digits, m, l, mh, lh) ? 1 : 0;
-        o.dec4 = acos_floor<4>(c.x, digits, m, l, mh, lh) ? 1 : 0;
+        o.dec2 = acos_floor<2>(xb, digits, m, l, mh, lh) ? 1 : 0;
+        o.dec4 = acos_floor<4>(xb, digits, m, l, mh, lh) ? 1 : 0;
         if(o.dec4) {
             int bias = digits == 53 ? 1023 : 127;
             o.rd4 = (static_cast<std::uint64_t>(l - (64 * 4 - 3) + bias) << (digits - 1)) |
@@ -42,11 +44,11 @@ SID_ACOS_HD inline Out check_one(Case c) {
         }
     }
     if(c.is_float) {
-        o.rd = acos_rounded_bits<24>(c.x, false);
-        o.ru = acos_rounded_bits<24>(c.x, true);
+        o.rd = float_bits(acos_rd(float(c.x)));
+        o.ru = float_bits(acos_ru(float(c.x)));
     } else {
-        o.rd = acos_rounded_bits<53>(c.x, false);
-        o.ru = acos_rounded_bits<53>(c.x, true);
+        o.rd = bits_of(acos_rd(c.x));
+        o.ru = bits_of(acos_ru(c.x));
     }
     return o;
 }
