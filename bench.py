@@ -41,6 +41,10 @@ N_CUBOIDS = 1 << 24
 SEED = 0x5EED0001
 # algorithmic bytes per cuboid of the batch kernel: read 2*8*nargs, write 2*8*nargs + 1 verdict byte
 BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
+# DRAM bytes (read + write) of one k_eval_batch launch on this workload, from ncu
+# (profiles/k_eval_batch_one_subcontainer_2e24.md); traffic grows in proportion to the batch
+NCU_TRAFFIC_BYTES_2E24 = 1.461791e9 + 1.385948e9
+NCU_FP64_PIPE_ACTIVE = 0.835
 # kernels of one sid_eval_batch_device call: ordering keys + histogram, two block scans, scan add, bucket
 # scatter, evaluation
 LAUNCHES_PER_EVAL = 6
@@ -385,7 +389,8 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "cuboids/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind,
+                     "traffic": NCU_TRAFFIC_BYTES_2E24 * n / float(1 << 24), "peak_kind": peak_kind,
+                     "fp64_pipe_active_ncu": NCU_FP64_PIPE_ACTIVE,
                      "kernel": "k_eval_batch (one_subcontainer, Morton-ordered)",
                      "kernel_ms": kernel_s * 1000.0, "ordering_ms_per_step": order_ms / max(prof_calls, 1),
                      "note": "algorithmic bytes; the kernel is limited by the FP64 pipe, not HBM (see DESIGN.md)"},
