@@ -29,7 +29,7 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fPIC",
     "--fmad=false", "--ftz=false", "--prec-div=true", "--prec-sqrt=true",
     "-I" + CSRC, "-I" + os.path.join(REPO, "include"),
-]
+] + os.environ.get("SID_NVCC_DEFINES", "").split()   # e.g. "-DSID_FILTER_MIN_BLOCKS=6" for tuning builds
 
 
 def nvcc():

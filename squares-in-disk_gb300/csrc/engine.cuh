@@ -376,7 +376,10 @@ __device__ __forceinline__ void split_child_f32(float lb_lo, float ub_hi, float4
 /// contains the double child box. A child refuted in float is a leaf (interval arithmetic in float is as
 /// sound as in double); every other child id goes to the escalation list, whose children are then
 /// evaluated in double by k_level_esc, with double results used throughout.
-template<class L> __global__ void __launch_bounds__(128) k_filter_f32(const LevelArgs a) {
+#ifndef SID_FILTER_MIN_BLOCKS
+#define SID_FILTER_MIN_BLOCKS 8     // resident 128-thread blocks per SM the float pass is compiled for (64 registers)
+#endif
+template<class L> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) k_filter_f32(const LevelArgs a) {
     constexpr int N = L::NARGS;
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if(t >= a.n_child) return;
@@ -451,6 +454,7 @@ struct BatchArgs {
     std::int8_t* verdict;
     std::uint64_t n;
     const std::uint32_t* order;   // thread t evaluates cuboid order[t] (nullptr: cuboid t)
+    std::uint64_t stride;         // distance between variables in lo/hi/out_lo/out_hi (0: n)
 };
 
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
@@ -465,15 +469,16 @@ template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(c
     const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
     Iv<T> box[N];
     #pragma unroll
-    for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * a.n + i]), T(a.hi[std::uint64_t(v) * a.n + i]), false};
+    const std::uint64_t st = a.stride ? a.stride : a.n;
+    for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
     std::int8_t vd = 0;
     if(propagate<L, T>(N - 1, box, N, 4)) vd = 1;
     else if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
     a.verdict[i] = vd;
     #pragma unroll
     for(int v = 0; v < N; ++v) {
-        a.out_lo[std::uint64_t(v) * a.n + i] = double(box[v].lo);
-        a.out_hi[std::uint64_t(v) * a.n + i] = double(box[v].hi);
+        a.out_lo[std::uint64_t(v) * st + i] = double(box[v].lo);
+        a.out_hi[std::uint64_t(v) * st + i] = double(box[v].hi);
     }
 }
 
