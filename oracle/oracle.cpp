@@ -770,6 +770,93 @@ std::vector<double> root_box(const std::string& ir) {
     return r;
 }
 
+namespace {
+
+/// The expressions compared by the constraints' comparison nodes that are not decided at compile time:
+/// constraints in table order, each predicate tree in pre-order, (left, right) per comparison, every
+/// comparison node once.
+std::vector<int> comparison_operands(const LemmaIR& L) {
+    std::vector<int> out;
+    std::vector<char> seen(L.nodes.size(), 0);
+    std::vector<int> stack;
+    for(int root : L.constraints) {
+        stack.assign(1, root);
+        while(!stack.empty()) {
+            const int id = stack.back();
+            stack.pop_back();
+            if(seen[std::size_t(id)]) continue;
+            seen[std::size_t(id)] = 1;
+            const auto& nd = L.nodes[std::size_t(id)];
+            if(nd.lb == nd.ub) continue;   // decided at compile time
+            switch(nd.op) {
+                case NodeOp::Lt: case NodeOp::Le: case NodeOp::Gt: case NodeOp::Ge: case NodeOp::Eq: case NodeOp::Ne:
+                    out.push_back(nd.ch[0]);
+                    out.push_back(nd.ch[1]);
+                    break;
+                case NodeOp::OrSeq: case NodeOp::AndSeq: case NodeOp::Or: case NodeOp::And: case NodeOp::Not:
+                    for(std::size_t k = nd.ch.size(); k-- > 0;) stack.push_back(nd.ch[k]);
+                    break;
+                default: break;
+            }
+        }
+    }
+    return out;
+}
+
+template<class T> void eval_operands_t(const LemmaIR& L, const std::vector<int>& ops, const double* lo, const double* hi,
+                                       std::uint64_t n, double* out, std::int8_t* und, int threads) {
+    int nt = threads > 0 ? threads : int(std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<std::uint64_t> next{0};
+    std::exception_ptr err;
+    std::mutex em;
+    const std::size_t k = ops.size();
+    auto work = [&] {
+        try {
+            RoundDownScope rd;
+            Evaluator<T> ev(L);
+            std::vector<Iv<T>> box(std::size_t(L.nargs));
+            for(;;) {
+                std::uint64_t b = next.fetch_add(256);
+                if(b >= n) break;
+                for(std::uint64_t i = b; i < std::min<std::uint64_t>(n, b + 256); ++i) {
+                    for(int v = 0; v < L.nargs; ++v) {
+                        const double l = lo[std::uint64_t(v) * n + i], h = hi[std::uint64_t(v) * n + i];
+                        box[std::size_t(v)] = {static_cast<T>(l), -static_cast<T>(-h), false};   // outward
+                    }
+                    ev.begin(box.data());
+                    for(std::size_t j = 0; j < k; ++j) {
+                        Iv<T> r = ev.eval(ops[j]);
+                        out[(i * k + j) * 2] = double(r.lo);
+                        out[(i * k + j) * 2 + 1] = double(r.hi);
+                        und[i * k + j] = r.und ? 1 : 0;
+                    }
+                }
+            }
+        } catch(...) {
+            std::lock_guard<std::mutex> g(em);
+            if(!err) err = std::current_exception();
+        }
+    };
+    std::vector<std::thread> th;
+    for(int t = 0; t < nt; ++t) th.emplace_back(work);
+    for(auto& t : th) t.join();
+    if(err) std::rethrow_exception(err);
+}
+
+} // namespace
+
+std::vector<int> operand_nodes(const std::string& ir) {
+    return comparison_operands(sid::parse_lemma_ir(ir));
+}
+
+void eval_operands(const std::string& ir, const double* lo, const double* hi, std::uint64_t n, bool use_float,
+                   double* out, std::int8_t* und, int threads) {
+    LemmaIR L = sid::parse_lemma_ir(ir);
+    const std::vector<int> ops = comparison_operands(L);
+    if(use_float) eval_operands_t<float>(L, ops, lo, hi, n, out, und, threads);
+    else eval_operands_t<double>(L, ops, lo, hi, n, out, und, threads);
+}
+
 void eval_batch(const std::string& ir, const double* lo, const double* hi, std::uint64_t n,
                 double* out_lo, double* out_hi, std::int8_t* verdict, int threads) {
     LemmaIR L = sid::parse_lemma_ir(ir);

@@ -75,6 +75,15 @@ ProveResult prove(const std::string& ir, const ProveOptions& opt);
 void eval_batch(const std::string& ir, const double* lo, const double* hi, std::uint64_t n,
                 double* out_lo, double* out_hi, std::int8_t* verdict, int threads);
 
+/// Node ids of the expressions compared by the constraints' runtime comparisons (left, right per
+/// comparison; constraints in table order, predicate trees in pre-order).
+std::vector<int> operand_nodes(const std::string& ir);
+
+/// Those expressions evaluated on n raw boxes (SoA lo/hi, rounded outward to float when use_float): out
+/// receives (lo, hi) per box and operand, und the possibly-undefined flag.
+void eval_operands(const std::string& ir, const double* lo, const double* hi, std::uint64_t n, bool use_float,
+                   double* out, std::int8_t* und, int threads);
+
 /// Initial runtime box (2*nargs doubles).
 std::vector<double> root_box(const std::string& ir);
 

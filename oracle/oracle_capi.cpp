@@ -71,6 +71,30 @@ int sido_eval_batch(const char* ir, const double* lo, const double* hi, unsigned
     }
 }
 
+/* Operand expressions of the runtime comparisons: their node ids (cap entries at most; returns the count or
+ * -1), and their intervals on n boxes in float (use_float != 0) or double. */
+int sido_operand_nodes(const char* ir, int* ids, int cap) {
+    try {
+        std::vector<int> v = sido::operand_nodes(ir);
+        for(std::size_t i = 0; i < v.size() && int(i) < cap; ++i) ids[i] = v[i];
+        return int(v.size());
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
+int sido_eval_operands(const char* ir, const double* lo, const double* hi, unsigned long long n, int use_float,
+                       double* out, signed char* und, int threads) {
+    try {
+        sido::eval_operands(ir, lo, hi, n, use_float != 0, out, reinterpret_cast<std::int8_t*>(und), threads);
+        return 0;
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
 /* acos(x) rounded down (up == 0) or up, for double (n doubles) and float (n floats); 0 or -1. */
 int sido_acos_rounded(const double* x, unsigned long long n, int up, double* out) {
     try {

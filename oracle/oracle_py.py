@@ -36,6 +36,9 @@ def lib():
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         _lib.sido_last_error.restype = ctypes.c_char_p
         _lib.sido_acos_rounded.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
+        _lib.sido_operand_nodes.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int]
+        _lib.sido_eval_operands.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_ulonglong,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         _lib.sido_acos_rounded_f32.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
     return _lib
 
@@ -98,3 +101,27 @@ def acos_rounded(x, up, dtype=np.float64):
     if fn(x.ctypes.data, x.size, 1 if up else 0, out.ctypes.data) != 0:
         raise RuntimeError(_err())
     return out
+
+
+def operand_nodes(ir_text):
+    """Node ids of the expressions the constraints compare at run time (left, right per comparison)."""
+    ids = np.zeros(4096, dtype=np.int32)
+    k = lib().sido_operand_nodes(ir_text.encode(), ids.ctypes.data, len(ids))
+    if k < 0:
+        raise RuntimeError(_err())
+    return [int(x) for x in ids[:k]]
+
+
+def eval_operands(ir_text, lo, hi, use_float, threads=0):
+    """Intervals of those expressions on raw boxes (SoA lo/hi, shape (nargs, n)), in float or double:
+    returns (lohi array (n, k, 2), undefined flags (n, k))."""
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    n = lo.shape[1]
+    k = len(operand_nodes(ir_text))
+    out = np.empty((n, k, 2), dtype=np.float64)
+    und = np.empty((n, k), dtype=np.int8)
+    if lib().sido_eval_operands(ir_text.encode(), lo.ctypes.data, hi.ctypes.data, n, 1 if use_float else 0,
+                                out.ctypes.data, und.ctypes.data, threads) != 0:
+        raise RuntimeError(_err())
+    return out, und
