@@ -67,6 +67,10 @@ typedef void (*sid_progress_fn)(void* user, const sid_progress* progress);
                                            refutes a child FP64 would not (possible only through a
                                            different propagation order); float lemmas run plain. */
 
+#define SID_PRECISION_FP32_TUNED 2      /* the precision form with the lemma's autotuned configuration
+                                           (sid_lemma_autotune: step size, levels that use the float
+                                           pass); before tuning, as SID_PRECISION_FP32_ESCALATE */
+
 /* Settings of one proof; meaning as ivarp::ProverSettings (prover_input.hpp:124-159). */
 typedef struct sid_prove_opts {
     uint32_t generation_count;          /* default 8 */
@@ -80,6 +84,8 @@ typedef struct sid_prove_opts {
     void* progress_user;
     uint32_t progress_first_ms;         /* delay before the first callback */
     uint32_t progress_every_ms;
+    uint32_t fp32_level_mask;           /* precision forms: levels that use the float pass (default all;
+                                           SID_PRECISION_FP32_TUNED uses the lemma's tuned mask) */
 } sid_prove_opts;
 
 /* Fill `opts` with the defaults above. */
@@ -109,6 +115,28 @@ int sid_prove(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, sid_
 /* Copy the criticals retained by the last sid_prove of this lemma: n*2*nargs doubles, per critical
  * the (lo,hi) pairs of all variables (the on_critical calls of cpu_prover_core.hpp:137-149). */
 int sid_fetch_criticals(sid_engine* engine, int lemma_id, double* out, uint64_t capacity, uint64_t* n_out);
+
+/* Autotuning of the precision form for one lemma (no counterpart in the reference). Levels are numbered
+ * dynamic splits first (root partition and re-splits of dynamic variable d share level d), then static
+ * splits (level D + j). A first precision-form proof measures each level's escalation rate (children the
+ * float pass cannot refute / children); candidate configurations combine a threshold (levels whose rate
+ * exceeds it skip the float pass and go straight to double) with a step size, and are timed by proving
+ * the lemma, as long as max_seconds of proving allows. Every candidate must reproduce the first proof's
+ * cuboid, leaf and critical counts or it is discarded. The fastest is stored with the lemma and used by
+ * SID_PRECISION_FP32_TUNED proofs and servers. */
+#define SID_MAX_LEVELS 16
+typedef struct sid_tuning {
+    int64_t step_elements;                    /* queue elements per step */
+    uint32_t fp32_level_mask;                 /* bit l set: level l uses the float pass */
+    float escalation_threshold;               /* the threshold the mask came from */
+    int32_t levels;                           /* dynamic + static levels of the lemma */
+    uint32_t candidates;                      /* configurations timed */
+    double level_escalation[SID_MAX_LEVELS];  /* measured escalation rate per level (-1: no children) */
+    double seconds;                           /* proof time with the chosen configuration */
+    double default_seconds;                   /* proof time with every level on the float pass, 65536 per step */
+} sid_tuning;
+
+int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid_tuning* out);
 
 /* Leaf evaluation of a batch of cuboids: for each cuboid, propagate the bounds after a change of the
  * last variable (it_limit = nargs, rec_limit = 4) and test all constraints -- the innermost step of

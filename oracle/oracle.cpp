@@ -533,8 +533,9 @@ template<class T> struct Driver {
     /// that contains the double child range: lo = RD(RD(lb) + RD(i*RD(w))), hi = RU(RU(lb) + RU((i+1)*RU(w))),
     /// the last child ending at RU(ub)), then the same propagation and constraint rows as the double path.
     bool refuted_in_fp32(Provers<T>& S, Counts& c, const std::vector<Iv<T>>& parent, int arg, int i, int n,
-                         std::size_t it, unsigned rec, int r0, int r1) {
+                         std::size_t it, unsigned rec, int r0, int r1, std::size_t level) {
         if(!S.F) return false;
+        if(level < 32 && !((opt.fp32_level_mask >> level) & 1u)) return false;   // level without the float pass
         std::vector<Iv<float>>& fb = fbox;
         fb.resize(parent.size());
         // the ambient rounding mode is downward: a cast rounds down, -cast(-x) rounds up
@@ -573,7 +574,7 @@ template<class T> struct Driver {
             split_point_pair(box[std::size_t(s.arg)].lo, box[std::size_t(s.arg)].hi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
             if(refuted_in_fp32(S, c, box, s.arg, i, m, 2 * std::size_t(L.nargs), rec_limit,
-                               d + 1 == dyn.size() ? L.nargs - 1 : 0, d + 1 == dyn.size() ? L.nargs : 0)) {
+                               d + 1 == dyn.size() ? L.nargs - 1 : 0, d + 1 == dyn.size() ? L.nargs : 0, d)) {
                 ++c.leaves;
                 continue;
             }
@@ -620,7 +621,10 @@ template<class T> struct Driver {
             T lo, hi;
             split_point_pair(plo, phi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
-            if(refuted_in_fp32(S, c, box, s.arg, i, m, std::size_t(L.nargs), 4, r0, r1)) { ++c.leaves; continue; }
+            if(refuted_in_fp32(S, c, box, s.arg, i, m, std::size_t(L.nargs), 4, r0, r1, dyn.size() + j)) {
+                ++c.leaves;
+                continue;
+            }
             if(P.propagate(s.arg, child.data(), std::size_t(L.nargs), 4)) { ++c.leaves; continue; }
             if(!P.rows_ok(r0, r1, child.data())) { ++c.leaves; continue; }
             handle(S, c, j + 1, child, hull);
@@ -660,7 +664,7 @@ template<class T> struct Driver {
             split_point_pair(box[std::size_t(s.arg)].lo, box[std::size_t(s.arg)].hi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
             if(refuted_in_fp32(S, c, box, s.arg, i, m, 2 * std::size_t(L.nargs), rec_limit,
-                               d + 1 == dyn.size() ? L.nargs - 1 : 0, d + 1 == dyn.size() ? L.nargs : 0)) {
+                               d + 1 == dyn.size() ? L.nargs - 1 : 0, d + 1 == dyn.size() ? L.nargs : 0, d)) {
                 ++c.leaves;
                 continue;
             }

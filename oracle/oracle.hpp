@@ -59,6 +59,8 @@ struct ProveOptions {
     bool fp32_first = false;         // precision form (double lemmas): children are first evaluated in
                                      // float, rounded outward; only those float cannot refute are
                                      // evaluated in double, whose results are used
+    std::uint32_t fp32_level_mask = ~0u;  // precision form: levels that use the float pass (bit d: dynamic
+                                          // level d, bit D + j: static level j)
 };
 
 struct ProveResult {

@@ -157,6 +157,8 @@ struct Lemma {
     const sid::LemmaKernels* k = nullptr;
     DevBuf<double2> root;                // initial runtime box, computed once at registration
     std::vector<double> root_host;       // the same, (lo, hi) per variable
+    bool tuned = false;                  // sid_lemma_autotune has chosen the precision-form configuration
+    sid_tuning tuning{};
     std::vector<double> criticals;       // from the last sid_prove
 };
 
@@ -371,6 +373,8 @@ __global__ void k_order_scatter(const std::uint32_t* key, std::uint64_t n, std::
     order[atomicAdd(&offset[key[i]], 1u)] = std::uint32_t(i);
 }
 
+__global__ void k_add_counter(unsigned long long* dst, const unsigned long long* src) { *dst += *src; }
+
 struct GatherEntry {
     std::uint32_t slot;
     std::uint32_t pad;
@@ -408,6 +412,7 @@ struct Lane {
     std::vector<IrSplit> dyn, stat;
     std::uint64_t step_cap = kDefaultStep;
     bool fp32_first = false;
+    std::uint32_t fp32_mask = ~0u;         // levels (dynamic d, static D + j) that use the float pass
     std::uint64_t fanout = 1, root_fanout = 1;
     int sm_count = 1;
     int max_slots = kDefaultSlots;
@@ -425,6 +430,8 @@ struct Lane {
     DevBuf<GatherEntry> gather;
     std::vector<GatherEntry> gather_host;
     long long grown_bytes = 0;             // device bytes request queues grew by since the last take_grown_bytes
+    DevBuf<unsigned long long> level_esc;  // escalated children per level (float pass), for tuning
+    std::vector<unsigned long long> level_children;
 
     Lane(sid_engine* e, Lemma* l, cudaStream_t s, bool own, int sms, int slots)
         : eng(e), lem(l), st(s), own_stream(own), sm_count(sms), max_slots(slots) {
@@ -450,9 +457,13 @@ struct Lane {
         if(own_stream && st) cudaStreamDestroy(st);
     }
 
-    void configure(std::uint64_t step_elements, bool fp32) {
+    void configure(std::uint64_t step_elements, bool fp32, std::uint32_t mask = ~0u) {
         step_cap = step_elements > 0 ? step_elements : kDefaultStep;
         fp32_first = fp32 && lem->k->filter_f32 != nullptr;
+        fp32_mask = mask;
+        level_esc.reserve(SID_MAX_LEVELS);
+        cuda_check(cudaMemsetAsync(level_esc.p, 0, SID_MAX_LEVELS * sizeof(unsigned long long), st), "level stats");
+        level_children.assign(SID_MAX_LEVELS, 0);
         hull.reserve(4 * step_cap * std::uint64_t(n));
         step.reserve(n, std::max(step.cap, step_cap), false, false, true, true);
         fin.reserve(n, std::max(fin.cap, step_cap), false, false, true, true);
@@ -598,10 +609,23 @@ struct Lane {
         return a;
     }
 
-    void launch(int mode, const LevelArgs& a0) {
+    /// Per-level escalation counts since configure(): (children, escalated) per level.
+    std::vector<std::pair<unsigned long long, unsigned long long>> level_stats() {
+        std::vector<unsigned long long> esc_h(SID_MAX_LEVELS, 0);
+        cuda_check(cudaMemcpyAsync(esc_h.data(), level_esc.p, SID_MAX_LEVELS * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, st), "level stats");
+        cuda_check(cudaStreamSynchronize(st), "level stats");
+        std::vector<std::pair<unsigned long long, unsigned long long>> out;
+        for(int l = 0; l < SID_MAX_LEVELS; ++l) out.emplace_back(level_children[std::size_t(l)], esc_h[std::size_t(l)]);
+        return out;
+    }
+
+    void launch(int mode, const LevelArgs& a0, int level) {
         const std::uint64_t total = a0.n_in * std::uint64_t(a0.nsub);
         if(total == 0) return;
-        if(!fp32_first) {
+        const bool level_fp32 = fp32_first && level < SID_MAX_LEVELS && ((fp32_mask >> level) & 1u);
+        if(level_fp32) level_children[std::size_t(level)] += total;
+        if(!level_fp32) {
             LevelArgs a = a0;
             a.count_cuboids = true;
             cuda_check(lem->k->level(mode, a, st), "level kernel launch");
@@ -630,6 +654,7 @@ struct Lane {
             a.pitem_begin = first;
             cuda_check(cudaMemsetAsync(a.esc_count, 0, sizeof(unsigned long long), st), "reset escalation count");
             cuda_check(lem->k->filter_f32(a, st), "float pass launch");
+            k_add_counter<<<1, 1, 0, st>>>(level_esc.p + level, a.esc_count);
             const std::uint64_t want = (a.n_child + 127) / 128;
             const unsigned blocks = unsigned(std::min<std::uint64_t>(want, std::uint64_t(sm_count) * kEscBlocksPerSM));
             cuda_check(lem->k->level_esc(mode, a, blocks, st), "escalated pass launch");
@@ -683,7 +708,7 @@ struct Lane {
                 a.row_begin = n - 1;
                 a.row_end = n;
                 a.depth_add = depth_add;
-                launch(MODE_QUEUE, a);
+                launch(MODE_QUEUE, a, int(d));
             } else {
                 a.row_begin = a.row_end = 0;
                 a.out_box = out->box.p;
@@ -692,7 +717,7 @@ struct Lane {
                 a.out_depth = out->depth.p;
                 a.out_tag = out->tag.p;
                 set_counter(counters.p, 0);
-                launch(MODE_EMIT, a);
+                launch(MODE_EMIT, a, int(d));
                 std::uint64_t cnt = read_counter(counters.p);
                 run_dynamic(d + 1, out->box.p, out->cap, out->depth.p, out->tag.p, 0, 0, cnt, initial, depth_add);
             }
@@ -721,7 +746,7 @@ struct Lane {
                 a.hull_hi = hull.p + step_cap * n;
                 a.hull_zlo = hull.p + 2 * step_cap * n;
                 a.hull_zhi = hull.p + 3 * step_cap * n;
-                launch(final_mode, a);
+                launch(final_mode, a, int(dyn.size() + j));
             }
             return;
         }
@@ -740,7 +765,7 @@ struct Lane {
             a.out_box = out.box.p; a.out_stride = out.cap; a.out_cap = out.cap;
             a.out_elem = out.elem.p; a.out_path = out.path.p;
             set_counter(counters.p, 0);
-            launch(MODE_EMIT, a);
+            launch(MODE_EMIT, a, int(dyn.size() + j));
             std::uint64_t cnt = read_counter(counters.p);
             run_static(j + 1, out.box.p, out.cap, out.elem.p, out.path.p, elem_tag, 0, cnt, final_mode);
         }
@@ -929,13 +954,16 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
 constexpr std::uint64_t kBatchChunk = std::uint64_t(1) << 20;   // cuboids per transfer chunk of sid_eval_batch
 
 void check_precision(int precision) {
-    if(precision != SID_PRECISION_PLAIN && precision != SID_PRECISION_FP32_ESCALATE) {
+    if(precision != SID_PRECISION_PLAIN && precision != SID_PRECISION_FP32_ESCALATE &&
+       precision != SID_PRECISION_FP32_TUNED) {
         fail(SID_ERR_INVALID, "unknown precision mode %d", precision);
     }
 }
 
-/// A whole proof of one lemma (sid_prove): one request on the engine's lane of that lemma.
-void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_result* res) {
+/// A whole proof of one lemma (sid_prove): one request on the engine's lane of that lemma. A non-zero
+/// step/mask override the step size and the float-pass levels (autotuning).
+void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_result* res, std::uint64_t step_override = 0,
+               const std::uint32_t* mask_override = nullptr) {
     Lemma* lem = get_lemma(eng, lemma_id);
     if(o.max_iterations_per_node > 1) {
         fail(SID_ERR_UNSUPPORTED, "max_iterations_per_node > 1 (re-iteration of a node) is not supported; use 1");
@@ -943,8 +971,11 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
     auto& slot = eng->prove_lanes[lemma_id];
     if(!slot) slot.reset(new Lane(eng, lem, eng->stream, false, eng->sm_count, 1));
     Lane& lane = *slot;
-    lane.configure(o.batch_elements > 0 ? std::uint64_t(o.batch_elements) : kDefaultStep,
-                   o.precision == SID_PRECISION_FP32_ESCALATE);
+    const bool tuned = o.precision == SID_PRECISION_FP32_TUNED && lem->tuned;
+    const std::uint64_t step = o.batch_elements > 0 ? std::uint64_t(o.batch_elements)
+                                                    : (tuned ? std::uint64_t(lem->tuning.step_elements) : kDefaultStep);
+    lane.configure(step_override ? step_override : step, o.precision != SID_PRECISION_PLAIN,
+                   mask_override ? *mask_override : (tuned ? lem->tuning.fp32_level_mask : o.fp32_level_mask));
 
     Request r;
     r.lem = lem;
@@ -1063,8 +1094,10 @@ struct sid_server {
             Lemma* lem = eng->lemmas[std::size_t(w->lemma_id)].get();
             const int slots = int(opts.max_requests_per_lane > 0 ? opts.max_requests_per_lane : kDefaultSlots);
             w->lane.reset(new Lane(eng, lem, s, true, eng->sm_count, slots));
-            w->lane->configure(opts.step_elements > 0 ? std::uint64_t(opts.step_elements) : kDefaultStep,
-                               opts.precision == SID_PRECISION_FP32_ESCALATE);
+            const bool tuned = opts.precision == SID_PRECISION_FP32_TUNED && lem->tuned;
+            w->lane->configure(opts.step_elements > 0 ? std::uint64_t(opts.step_elements)
+                                                      : (tuned ? std::uint64_t(lem->tuning.step_elements) : kDefaultStep),
+                               opts.precision != SID_PRECISION_PLAIN, tuned ? lem->tuning.fp32_level_mask : ~0u);
             Lane& lane = *w->lane;
             for(;;) {
                 std::vector<Request*> admit;
@@ -1179,6 +1212,7 @@ void sid_prove_opts_default(sid_prove_opts* o) {
     o->max_criticals_kept = 1u << 20;
     o->progress_first_ms = 8000;
     o->progress_every_ms = 2000;
+    o->fp32_level_mask = ~0u;
 }
 
 const char* sid_last_error(void) { return g_last_error; }
@@ -1368,6 +1402,88 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
             throw;
         }
         for(cudaEvent_t e : evs) cudaEventDestroy(e);
+    });
+}
+
+int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid_tuning* out) {
+    return guarded([&] {
+        Lemma* l = get_lemma(engine, lemma_id);
+        if(!out) fail(SID_ERR_INVALID, "null output");
+        set_device(engine);
+        sid_tuning t{};
+        t.step_elements = std::int64_t(kDefaultStep);
+        t.fp32_level_mask = ~0u;
+        t.escalation_threshold = 1.01f;
+        const int levels = int(l->ir.dynamic_splits().size() + l->ir.static_splits().size());
+        t.levels = levels;
+        for(int k = 0; k < SID_MAX_LEVELS; ++k) t.level_escalation[k] = -1.0;
+        sid_prove_opts o;
+        sid_prove_opts_default(&o);
+        o.precision = SID_PRECISION_FP32_ESCALATE;
+        o.max_criticals_kept = 0;
+        double spent = 0;
+        auto timed = [&](std::uint64_t step, std::uint32_t mask, sid_result& best) {
+            for(int rep = 0; rep < 2; ++rep) {
+                sid_result r{};
+                prove_one(engine, lemma_id, o, &r, step, &mask);
+                spent += r.seconds;
+                if(rep == 0 || r.seconds < best.seconds) best = r;
+            }
+        };
+        // baseline: every level on the float pass, the default step; per-level escalation rates
+        sid_result base{};
+        const std::uint32_t all = ~0u;
+        timed(kDefaultStep, all, base);
+        t.default_seconds = base.seconds;
+        t.seconds = base.seconds;
+        t.candidates = 1;
+        if(l->k->filter_f32 != nullptr) {
+            const auto stats = engine->prove_lanes[lemma_id]->level_stats();
+            for(int k = 0; k < std::min(levels, SID_MAX_LEVELS); ++k) {
+                if(stats[std::size_t(k)].first) {
+                    t.level_escalation[k] = double(stats[std::size_t(k)].second) / double(stats[std::size_t(k)].first);
+                }
+            }
+            auto same = [&](const sid_result& r) {
+                return r.num_cuboids == base.num_cuboids && r.num_leaf_cuboids == base.num_leaf_cuboids &&
+                       r.num_critical_cuboids == base.num_critical_cuboids;
+            };
+            // candidate masks from thresholds on the measured rates
+            std::vector<std::pair<float, std::uint32_t>> masks;
+            for(float thr : {0.95f, 0.8f, 0.6f}) {
+                std::uint32_t m = ~0u;
+                for(int k = 0; k < std::min(levels, SID_MAX_LEVELS); ++k) {
+                    if(t.level_escalation[k] > double(thr)) m &= ~(1u << k);
+                }
+                bool seen = m == all;
+                for(const auto& e : masks) seen = seen || e.second == m;
+                if(!seen) masks.emplace_back(thr, m);
+            }
+            for(const auto& cand : masks) {
+                if(spent > max_seconds) break;
+                sid_result r{};
+                timed(kDefaultStep, cand.second, r);
+                ++t.candidates;
+                if(same(r) && r.seconds < t.seconds) {
+                    t.seconds = r.seconds;
+                    t.fp32_level_mask = cand.second;
+                    t.escalation_threshold = cand.first;
+                }
+            }
+            for(std::uint64_t step : {std::uint64_t(1) << 15, std::uint64_t(1) << 17, std::uint64_t(1) << 14}) {
+                if(spent > max_seconds) break;
+                sid_result r{};
+                timed(step, t.fp32_level_mask, r);
+                ++t.candidates;
+                if(same(r) && r.seconds < t.seconds) {
+                    t.seconds = r.seconds;
+                    t.step_elements = std::int64_t(step);
+                }
+            }
+        }
+        l->tuning = t;
+        l->tuned = true;
+        *out = t;
     });
 }
 

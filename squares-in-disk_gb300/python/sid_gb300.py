@@ -23,9 +23,11 @@ EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "si
             "sid_lemma_register", "sid_lemma_info", "sid_lemma_root_box", "sid_prove", "sid_fetch_criticals",
             "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc", "sid_server_opts_default",
             "sid_server_create", "sid_server_destroy", "sid_submit", "sid_request_poll", "sid_request_wait",
-            "sid_request_criticals", "sid_request_release", "sid_eval_batch_profile", "sid_eval_batch_profile_read"]
+            "sid_request_criticals", "sid_request_release", "sid_eval_batch_profile", "sid_eval_batch_profile_read",
+            "sid_lemma_autotune"]
 
-PRECISION_PLAIN, PRECISION_FP32 = 0, 1
+PRECISION_PLAIN, PRECISION_FP32, PRECISION_TUNED = 0, 1, 2
+MAX_LEVELS = 16
 REQ_PENDING, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 
@@ -45,7 +47,7 @@ class SidProveOpts(ctypes.Structure):
                 ("batch_elements", ctypes.c_int64), ("precision", ctypes.c_int32),
                 ("max_criticals_kept", ctypes.c_uint64), ("progress", ctypes.c_void_p),
                 ("progress_user", ctypes.c_void_p), ("progress_first_ms", ctypes.c_uint32),
-                ("progress_every_ms", ctypes.c_uint32)]
+                ("progress_every_ms", ctypes.c_uint32), ("fp32_level_mask", ctypes.c_uint32)]
 
 
 class SidServerOpts(ctypes.Structure):
@@ -65,6 +67,13 @@ class SidRequestStatus(ctypes.Structure):
                     leaves=self.num_leaf_cuboids, criticals=self.num_critical_cuboids, escalated=self.escalated,
                     stored=self.criticals_stored, seconds_queued=self.seconds_queued,
                     seconds_to_verdict=self.seconds_to_verdict)
+
+
+class SidTuning(ctypes.Structure):
+    _fields_ = [("step_elements", ctypes.c_int64), ("fp32_level_mask", ctypes.c_uint32),
+                ("escalation_threshold", ctypes.c_float), ("levels", ctypes.c_int32), ("candidates", ctypes.c_uint32),
+                ("level_escalation", ctypes.c_double * MAX_LEVELS), ("seconds", ctypes.c_double),
+                ("default_seconds", ctypes.c_double)]
 
 
 class SidError(RuntimeError):
@@ -112,6 +121,7 @@ def load(path=LIB_PATH):
                                         ctypes.POINTER(ctypes.c_uint64)]
     L.sid_request_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
     L.sid_eval_batch_profile.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.sid_lemma_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.POINTER(SidTuning)]
     L.sid_eval_batch_profile_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     _lib = L
@@ -182,7 +192,7 @@ class Engine:
         return out.reshape(nargs, 2)
 
     def prove(self, lemma_id, generations=8, max_iterations=1, max_criticals=1 << 20, batch=0, precision=0,
-              nargs=None, fetch=False):
+              nargs=None, fetch=False, fp32_level_mask=0xFFFFFFFF):
         opts = SidProveOpts()
         self.L.sid_prove_opts_default(ctypes.byref(opts))
         opts.generation_count = generations
@@ -190,6 +200,7 @@ class Engine:
         opts.max_criticals_kept = max_criticals
         opts.batch_elements = batch
         opts.precision = precision
+        opts.fp32_level_mask = fp32_level_mask
         res = SidResult()
         _check(self.L.sid_prove(self.h, lemma_id, ctypes.byref(opts), ctypes.byref(res)))
         out = dict(cuboids=res.num_cuboids, leaves=res.num_leaf_cuboids, criticals=res.num_critical_cuboids,
@@ -218,6 +229,15 @@ class Engine:
         _check(self.L.sid_eval_batch_device(self.h, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr,
                                             verdict_ptr, stream))
 
+
+    def autotune(self, lemma_id, max_seconds=5.0):
+        """Choose the precision form's step size and float-pass levels for a lemma (sid_lemma_autotune)."""
+        t = SidTuning()
+        _check(self.L.sid_lemma_autotune(self.h, lemma_id, max_seconds, ctypes.byref(t)))
+        return dict(step_elements=t.step_elements, fp32_level_mask=t.fp32_level_mask,
+                    escalation_threshold=t.escalation_threshold, levels=t.levels, candidates=t.candidates,
+                    level_escalation=[t.level_escalation[k] for k in range(min(t.levels, MAX_LEVELS))],
+                    seconds=t.seconds, default_seconds=t.default_seconds)
 
     def batch_profile(self, enable):
         """Record CUDA events around the ordering and evaluation kernels of the following batch calls."""
