@@ -139,7 +139,8 @@ def cpu_baseline(ir, lo, hi, threads, budget_s=1.5):
     return sample, dt
 
 
-PRECISION_PLAIN, PRECISION_FP32 = 0, 1
+PRECISION_PLAIN, PRECISION_FP32, PRECISION_TUNED = 0, 1, 2
+TUNE_SECONDS = 2.0            # autotuning budget per lemma (seconds of proving)
 PUBLISHED = os.path.join(REPO, "tests", "golden", "published_counts.json")
 
 
@@ -162,8 +163,18 @@ def prove_lemma_set(eng, sid, repeats=2):
             if prec == PRECISION_FP32:
                 row[key]["escalated"] = r["escalated"]
                 row[key]["escalation_rate"] = r["escalated"] / max(r["cuboids"], 1)
+        tune = eng.autotune(lid, max_seconds=TUNE_SECONDS)
+        runs = [eng.prove(lid, precision=PRECISION_TUNED) for _ in range(repeats)]
+        r = min(runs, key=lambda x: x["seconds"])
+        row["tuned"] = {"cuboids": r["cuboids"], "leaves": r["leaves"], "criticals": r["criticals"],
+                        "seconds": r["seconds"], "cuboids_per_s": r["cuboids"] / max(r["seconds"], 1e-9),
+                        "escalated": r["escalated"], "step_elements": tune["step_elements"],
+                        "fp32_level_mask": tune["fp32_level_mask"], "level_escalation": tune["level_escalation"],
+                        "candidates": tune["candidates"]}
+        tot["tuned_s"] = tot.get("tuned_s", 0.0) + r["seconds"]
         pub = published.get(name) or [None, None]
         row["delta_cuboids_fp32_vs_published"] = None if pub[0] is None else row["fp32"]["cuboids"] - pub[0]
+        row["delta_cuboids_tuned_vs_published"] = None if pub[0] is None else row["tuned"]["cuboids"] - pub[0]
         row["plain_matches_published"] = [row["plain"]["cuboids"], row["plain"]["leaves"]] == pub
         row["speedup_fp32_vs_plain"] = row["plain"]["seconds"] / max(row["fp32"]["seconds"], 1e-9)
         tot["plain_s"] += row["plain"]["seconds"]
@@ -173,7 +184,9 @@ def prove_lemma_set(eng, sid, repeats=2):
     out["_total"] = {"cuboids": tot["cuboids"], "plain_seconds": tot["plain_s"], "fp32_seconds": tot["fp32_s"],
                      "plain_cuboids_per_s": tot["cuboids"] / max(tot["plain_s"], 1e-9),
                      "fp32_cuboids_per_s": tot["cuboids"] / max(tot["fp32_s"], 1e-9),
-                     "speedup_fp32_vs_plain": tot["plain_s"] / max(tot["fp32_s"], 1e-9)}
+                     "speedup_fp32_vs_plain": tot["plain_s"] / max(tot["fp32_s"], 1e-9),
+                     "tuned_seconds": tot.get("tuned_s"), "tuned_cuboids_per_s": tot["cuboids"] / max(tot.get("tuned_s", 1e-9), 1e-9),
+                     "speedup_tuned_vs_plain": tot["plain_s"] / max(tot.get("tuned_s", 1e-9), 1e-9)}
     return out
 
 
