@@ -46,6 +46,8 @@ typedef struct sid_result {
     uint64_t criticals_stored;   /* criticals retained for sid_fetch_criticals */
     uint64_t escalated;          /* cuboids re-evaluated in FP64 (precision form only) */
     double seconds;              /* device wall time of the proof */
+    int32_t complete;            /* 0 if the proof stopped early at a checkpoint (opts.stop_after_steps) */
+    uint32_t steps;              /* steps run (queue batches expanded) */
 } sid_result;
 
 /* Snapshot handed to a progress callback (ivarp::ProgressInfo, default_progress_observer.hpp:30-35). */
@@ -86,6 +88,10 @@ typedef struct sid_prove_opts {
     uint32_t progress_every_ms;
     uint32_t fp32_level_mask;           /* precision forms: levels that use the float pass (default all;
                                            SID_PRECISION_FP32_TUNED uses the lemma's tuned mask) */
+    const char* checkpoint_path;        /* if set: write the proof's state to this file every
+                                           checkpoint_every_steps steps and when stopping early */
+    uint32_t checkpoint_every_steps;    /* 0: only when stopping early */
+    uint32_t stop_after_steps;          /* > 0: stop after this many steps (with a checkpoint) */
 } sid_prove_opts;
 
 /* Fill `opts` with the defaults above. */
@@ -111,6 +117,13 @@ int sid_lemma_root_box(sid_engine* engine, int lemma_id, double* out_lohi);
 /* Run a whole proof (ProofDriver::run, proof_driver.hpp:472-489). Returns SID_OK whether or not
  * criticals remain; the verdict is result->num_critical_cuboids == 0. */
 int sid_prove(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, sid_result* result);
+
+/* Continue a proof from a checkpoint written by sid_prove (no counterpart in the reference). The file holds
+ * the lemma's fingerprint, the generation limit, the counters and stored criticals, and the frontier queue
+ * (boxes and depths) between two steps; the result counts the whole proof, so a resumed proof reports what
+ * the uninterrupted one would. opts may checkpoint and stop again. */
+int sid_prove_resume(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, const char* checkpoint_path,
+                     sid_result* result);
 
 /* Copy the criticals retained by the last sid_prove of this lemma: n*2*nargs doubles, per critical
  * the (lo,hi) pairs of all variables (the on_critical calls of cpu_prover_core.hpp:137-149). */

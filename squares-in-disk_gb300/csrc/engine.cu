@@ -164,6 +164,16 @@ struct Lemma {
 
 using Clock = std::chrono::steady_clock;
 
+/// The state of a proof between two steps, as a checkpoint file holds it.
+struct ProofState {
+    std::uint64_t fingerprint = 0;
+    std::uint32_t nargs = 0, generations = 0, steps = 0;
+    std::uint64_t cnt[sid::RC_N] = {};
+    std::vector<double2> boxes;          // variable-major: boxes[v * qsize + i]
+    std::vector<std::uint8_t> depth;
+    std::vector<double> criticals;       // stored criticals, 2*nargs doubles each
+};
+
 /// One request: a whole-lemma proof or a set of sub-boxes, with its device frontier and results.
 /// The lane thread owns the device parts; `view`, `state` and the times are shared under the server lock.
 struct Request {
@@ -172,6 +182,7 @@ struct Request {
     Lemma* lem = nullptr;
     int slot = -1;
     bool full = true;                    // whole lemma (root partition) or sub-boxes
+    const ProofState* resume = nullptr;  // continue from a checkpoint instead
     std::vector<double> boxes;           // sub-boxes, box-major (lo, hi) pairs
     std::uint64_t nboxes = 0;
     unsigned generations = 8;
@@ -497,6 +508,7 @@ struct Lane {
     }
 
     std::uint64_t initial_queue_cap(const Request& r) const {
+        if(r.resume) return std::max<std::uint64_t>(r.resume->cnt[RC_QSIZE], 64);
         return std::max<std::uint64_t>(r.full ? root_fanout : r.nboxes, 64);
     }
     /// Device bytes a request holds right after admission.
@@ -537,7 +549,22 @@ struct Lane {
         h.crit = r->crit.p;
         h.crit_cap = r->crit_cap;
         h.generations = r->generations;
-        if(!r->full) {
+        if(r->resume) {
+            const ProofState& ps = *r->resume;
+            const std::uint64_t q = ps.cnt[RC_QSIZE];
+            std::memcpy(h.cnt, ps.cnt, sizeof(h.cnt));
+            for(int v = 0; v < n; ++v) {
+                cuda_check(cudaMemcpyAsync(r->qbox.p + std::uint64_t(v) * r->qcap, ps.boxes.data() + std::uint64_t(v) * q,
+                                           q * sizeof(double2), cudaMemcpyHostToDevice, st), "resume upload");
+            }
+            cuda_check(cudaMemcpyAsync(r->qdepth.p, ps.depth.data(), std::size_t(q), cudaMemcpyHostToDevice, st), "resume upload");
+            const std::size_t keep = std::min(ps.criticals.size(), std::size_t(r->crit_cap) * 2 * std::size_t(n));
+            if(keep) {
+                cuda_check(cudaMemcpyAsync(r->crit.p, ps.criticals.data(), keep * sizeof(double), cudaMemcpyHostToDevice, st),
+                           "resume upload");
+            }
+            cuda_check(cudaStreamSynchronize(st), "resume upload");
+        } else if(!r->full) {
             h.cnt[RC_QSIZE] = r->nboxes;
             h.cnt[RC_CUBOIDS] = r->nboxes;
             std::vector<double2> col(std::size_t(r->nboxes));
@@ -554,7 +581,7 @@ struct Lane {
         }
         cuda_check(cudaMemcpyAsync(req_dev.p + slot, &h, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
         cuda_check(cudaStreamSynchronize(st), "request slot");
-        if(r->full) run_dynamic(0, lem->root.p, 1, nullptr, nullptr, std::uint32_t(slot), 0, 1, true, 0);
+        if(r->full && !r->resume) run_dynamic(0, lem->root.p, 1, nullptr, nullptr, std::uint32_t(slot), 0, 1, true, 0);
         read_slots();
     }
 
@@ -588,6 +615,28 @@ struct Lane {
             std::memcpy(req_host[std::size_t(i)].cnt, tmp[std::size_t(i)].cnt, sizeof(tmp[0].cnt));
             if(tmp[std::size_t(i)].cnt[RC_OVERFLOW]) fail(SID_ERR_CUDA, "internal error: a request queue overflowed");
         }
+    }
+
+    /// The request's state between steps: counters, frontier queue, stored criticals.
+    void snapshot(Request* r, ProofState& ps) {
+        const ReqDev& c = counters_of(r);
+        std::memcpy(ps.cnt, c.cnt, sizeof(ps.cnt));
+        const std::uint64_t q = c.cnt[RC_QSIZE];
+        ps.nargs = std::uint32_t(n);
+        ps.boxes.resize(std::size_t(q * std::uint64_t(n)));
+        ps.depth.resize(std::size_t(q));
+        for(int v = 0; v < n; ++v) {
+            cuda_check(cudaMemcpyAsync(ps.boxes.data() + std::uint64_t(v) * q, r->qbox.p + std::uint64_t(v) * r->qcap,
+                                       q * sizeof(double2), cudaMemcpyDeviceToHost, st), "checkpoint copy");
+        }
+        cuda_check(cudaMemcpyAsync(ps.depth.data(), r->qdepth.p, std::size_t(q), cudaMemcpyDeviceToHost, st), "checkpoint copy");
+        const std::uint64_t k = std::min<std::uint64_t>(c.cnt[RC_CRITICALS], r->crit_cap);
+        ps.criticals.resize(std::size_t(k * 2 * std::uint64_t(n)));
+        if(k) {
+            cuda_check(cudaMemcpyAsync(ps.criticals.data(), r->crit.p, ps.criticals.size() * sizeof(double),
+                                       cudaMemcpyDeviceToHost, st), "checkpoint copy");
+        }
+        cuda_check(cudaStreamSynchronize(st), "checkpoint copy");
     }
 
     /// Critical boxes stored for a request (after it finished).
@@ -960,10 +1009,57 @@ void check_precision(int precision) {
     }
 }
 
+constexpr char kCheckpointMagic[8] = {'S', 'I', 'D', 'C', 'K', 'P', 'T', '1'};
+
+void write_checkpoint(const char* path, const ProofState& ps) {
+    std::string tmp = std::string(path) + ".part";
+    std::FILE* f = std::fopen(tmp.c_str(), "wb");
+    if(!f) fail(SID_ERR_INVALID, "cannot write checkpoint %s", tmp.c_str());
+    const std::uint64_t q = ps.cnt[RC_QSIZE], crit = ps.criticals.size();
+    bool ok = std::fwrite(kCheckpointMagic, 1, 8, f) == 8 &&
+              std::fwrite(&ps.fingerprint, sizeof ps.fingerprint, 1, f) == 1 &&
+              std::fwrite(&ps.nargs, sizeof ps.nargs, 1, f) == 1 &&
+              std::fwrite(&ps.generations, sizeof ps.generations, 1, f) == 1 &&
+              std::fwrite(&ps.steps, sizeof ps.steps, 1, f) == 1 &&
+              std::fwrite(ps.cnt, sizeof ps.cnt, 1, f) == 1 &&
+              std::fwrite(&crit, sizeof crit, 1, f) == 1 &&
+              (q == 0 || std::fwrite(ps.boxes.data(), sizeof(double2), ps.boxes.size(), f) == ps.boxes.size()) &&
+              (q == 0 || std::fwrite(ps.depth.data(), 1, ps.depth.size(), f) == ps.depth.size()) &&
+              (crit == 0 || std::fwrite(ps.criticals.data(), sizeof(double), crit, f) == crit);
+    ok = (std::fclose(f) == 0) && ok;
+    if(!ok || std::rename(tmp.c_str(), path) != 0) fail(SID_ERR_INVALID, "writing checkpoint %s failed", path);
+}
+
+void read_checkpoint(const char* path, ProofState& ps) {
+    std::FILE* f = std::fopen(path, "rb");
+    if(!f) fail(SID_ERR_INVALID, "cannot open checkpoint %s", path);
+    char magic[8];
+    std::uint64_t crit = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kCheckpointMagic, 8) == 0 &&
+              std::fread(&ps.fingerprint, sizeof ps.fingerprint, 1, f) == 1 &&
+              std::fread(&ps.nargs, sizeof ps.nargs, 1, f) == 1 &&
+              std::fread(&ps.generations, sizeof ps.generations, 1, f) == 1 &&
+              std::fread(&ps.steps, sizeof ps.steps, 1, f) == 1 &&
+              std::fread(ps.cnt, sizeof ps.cnt, 1, f) == 1 && std::fread(&crit, sizeof crit, 1, f) == 1 &&
+              ps.nargs > 0 && ps.nargs <= 64 && ps.cnt[RC_QSIZE] <= (std::uint64_t(1) << 36) && crit <= (std::uint64_t(1) << 36);
+    if(ok) {
+        const std::uint64_t q = ps.cnt[RC_QSIZE];
+        ps.boxes.resize(std::size_t(q * ps.nargs));
+        ps.depth.resize(std::size_t(q));
+        ps.criticals.resize(std::size_t(crit));
+        ok = (q == 0 || std::fread(ps.boxes.data(), sizeof(double2), ps.boxes.size(), f) == ps.boxes.size()) &&
+             (q == 0 || std::fread(ps.depth.data(), 1, ps.depth.size(), f) == ps.depth.size()) &&
+             (crit == 0 || std::fread(ps.criticals.data(), sizeof(double), crit, f) == crit);
+    }
+    std::fclose(f);
+    if(!ok) fail(SID_ERR_INVALID, "%s is not a complete checkpoint", path);
+}
+
 /// A whole proof of one lemma (sid_prove): one request on the engine's lane of that lemma. A non-zero
-/// step/mask override the step size and the float-pass levels (autotuning).
+/// step/mask override the step size and the float-pass levels (autotuning); `resume` continues from a
+/// checkpoint.
 void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_result* res, std::uint64_t step_override = 0,
-               const std::uint32_t* mask_override = nullptr) {
+               const std::uint32_t* mask_override = nullptr, const ProofState* resume = nullptr) {
     Lemma* lem = get_lemma(eng, lemma_id);
     if(o.max_iterations_per_node > 1) {
         fail(SID_ERR_UNSUPPORTED, "max_iterations_per_node > 1 (re-iteration of a node) is not supported; use 1");
@@ -983,6 +1079,9 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
     r.full = true;
     r.generations = o.generation_count;
     r.crit_cap = o.max_criticals_kept;
+    r.resume = resume;
+    std::uint32_t steps = resume ? resume->steps : 0;
+    bool complete = true;
 
     cudaEvent_t ev0, ev1;
     cuda_check(cudaEventCreate(&ev0), "event");
@@ -995,8 +1094,26 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
         bool first_done = false;
         lane.admit(&r);
         const std::vector<Request*> active{&r};
+        auto checkpoint = [&]() {
+            ProofState ps;
+            lane.snapshot(&r, ps);
+            ps.fingerprint = lem->ir.fingerprint;
+            ps.generations = o.generation_count;
+            ps.steps = steps;
+            write_checkpoint(o.checkpoint_path, ps);
+        };
         while(lane.queue_size(&r) > 0) {
+            if(o.stop_after_steps && steps >= (resume ? resume->steps : 0) + o.stop_after_steps) {
+                complete = false;
+                if(o.checkpoint_path) checkpoint();
+                break;
+            }
             lane.run_step(active);
+            ++steps;
+            if(o.checkpoint_path && o.checkpoint_every_steps && steps % o.checkpoint_every_steps == 0 &&
+               lane.queue_size(&r) > 0) {
+                checkpoint();
+            }
             if(o.progress) {
                 const auto now = Clock::now();
                 const long long since_start = std::chrono::duration_cast<std::chrono::milliseconds>(now - t0).count();
@@ -1048,6 +1165,8 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
     res->criticals_stored = std::min<std::uint64_t>(res->num_critical_cuboids, r.crit_cap);
     res->escalated = last.cnt[RC_ESCALATED];
     res->seconds = double(ms) / 1000.0;
+    res->complete = complete ? 1 : 0;
+    res->steps = steps;
     lem->criticals = std::move(r.criticals);
 }
 
@@ -1312,6 +1431,27 @@ int sid_prove(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, sid_
         set_device(engine);
         std::memset(result, 0, sizeof(*result));
         prove_one(engine, lemma_id, o, result);
+    });
+}
+
+int sid_prove_resume(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, const char* checkpoint_path,
+                     sid_result* result) {
+    return guarded([&] {
+        Lemma* l = get_lemma(engine, lemma_id);
+        if(!result || !checkpoint_path) fail(SID_ERR_INVALID, "null argument");
+        sid_prove_opts o;
+        if(opts) o = *opts; else sid_prove_opts_default(&o);
+        check_precision(o.precision);
+        ProofState ps;
+        read_checkpoint(checkpoint_path, ps);
+        if(ps.fingerprint != l->ir.fingerprint) fail(SID_ERR_INVALID, "checkpoint %s belongs to another lemma", checkpoint_path);
+        if(int(ps.nargs) != l->ir.nargs) fail(SID_ERR_INVALID, "checkpoint %s has %u variables", checkpoint_path, ps.nargs);
+        if(ps.generations != o.generation_count) {
+            fail(SID_ERR_INVALID, "checkpoint %s was written with generation_count %u", checkpoint_path, ps.generations);
+        }
+        set_device(engine);
+        std::memset(result, 0, sizeof(*result));
+        prove_one(engine, lemma_id, o, result, 0, nullptr, &ps);
     });
 }
 

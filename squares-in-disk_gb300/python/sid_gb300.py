@@ -24,7 +24,7 @@ EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "si
             "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc", "sid_server_opts_default",
             "sid_server_create", "sid_server_destroy", "sid_submit", "sid_request_poll", "sid_request_wait",
             "sid_request_criticals", "sid_request_release", "sid_eval_batch_profile", "sid_eval_batch_profile_read",
-            "sid_lemma_autotune"]
+            "sid_lemma_autotune", "sid_prove_resume"]
 
 PRECISION_PLAIN, PRECISION_FP32, PRECISION_TUNED = 0, 1, 2
 MAX_LEVELS = 16
@@ -34,7 +34,8 @@ REQ_PENDING, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 class SidResult(ctypes.Structure):
     _fields_ = [("num_cuboids", ctypes.c_uint64), ("num_leaf_cuboids", ctypes.c_uint64),
                 ("num_critical_cuboids", ctypes.c_uint64), ("num_repeated_nodes", ctypes.c_uint64),
-                ("criticals_stored", ctypes.c_uint64), ("escalated", ctypes.c_uint64), ("seconds", ctypes.c_double)]
+                ("criticals_stored", ctypes.c_uint64), ("escalated", ctypes.c_uint64), ("seconds", ctypes.c_double),
+                ("complete", ctypes.c_int32), ("steps", ctypes.c_uint32)]
 
 
 PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p)
@@ -47,7 +48,9 @@ class SidProveOpts(ctypes.Structure):
                 ("batch_elements", ctypes.c_int64), ("precision", ctypes.c_int32),
                 ("max_criticals_kept", ctypes.c_uint64), ("progress", ctypes.c_void_p),
                 ("progress_user", ctypes.c_void_p), ("progress_first_ms", ctypes.c_uint32),
-                ("progress_every_ms", ctypes.c_uint32), ("fp32_level_mask", ctypes.c_uint32)]
+                ("progress_every_ms", ctypes.c_uint32), ("fp32_level_mask", ctypes.c_uint32),
+                ("checkpoint_path", ctypes.c_char_p), ("checkpoint_every_steps", ctypes.c_uint32),
+                ("stop_after_steps", ctypes.c_uint32)]
 
 
 class SidServerOpts(ctypes.Structure):
@@ -101,6 +104,8 @@ def load(path=LIB_PATH):
                                  ctypes.POINTER(ctypes.c_uint64)]
     L.sid_lemma_root_box.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     L.sid_prove.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(SidProveOpts), ctypes.POINTER(SidResult)]
+    L.sid_prove_resume.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(SidProveOpts), ctypes.c_char_p,
+                                   ctypes.POINTER(SidResult)]
     L.sid_fetch_criticals.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
                                       ctypes.POINTER(ctypes.c_uint64)]
     L.sid_eval_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
@@ -192,7 +197,10 @@ class Engine:
         return out.reshape(nargs, 2)
 
     def prove(self, lemma_id, generations=8, max_iterations=1, max_criticals=1 << 20, batch=0, precision=0,
-              nargs=None, fetch=False, fp32_level_mask=0xFFFFFFFF):
+              nargs=None, fetch=False, fp32_level_mask=0xFFFFFFFF, checkpoint=None, checkpoint_every=0, stop_after=0,
+              resume_from=None):
+        """A whole proof (sid_prove), or its continuation from a checkpoint file (resume_from, sid_prove_resume).
+        checkpoint/checkpoint_every/stop_after write checkpoints and stop early (result 'complete' False)."""
         opts = SidProveOpts()
         self.L.sid_prove_opts_default(ctypes.byref(opts))
         opts.generation_count = generations
@@ -201,11 +209,17 @@ class Engine:
         opts.batch_elements = batch
         opts.precision = precision
         opts.fp32_level_mask = fp32_level_mask
+        opts.checkpoint_path = checkpoint.encode() if checkpoint else None
+        opts.checkpoint_every_steps = checkpoint_every
+        opts.stop_after_steps = stop_after
         res = SidResult()
-        _check(self.L.sid_prove(self.h, lemma_id, ctypes.byref(opts), ctypes.byref(res)))
+        if resume_from:
+            _check(self.L.sid_prove_resume(self.h, lemma_id, ctypes.byref(opts), resume_from.encode(), ctypes.byref(res)))
+        else:
+            _check(self.L.sid_prove(self.h, lemma_id, ctypes.byref(opts), ctypes.byref(res)))
         out = dict(cuboids=res.num_cuboids, leaves=res.num_leaf_cuboids, criticals=res.num_critical_cuboids,
                    repeated=res.num_repeated_nodes, stored=res.criticals_stored, escalated=res.escalated,
-                   seconds=res.seconds)
+                   seconds=res.seconds, complete=bool(res.complete), steps=res.steps)
         if fetch and res.criticals_stored:
             buf = np.zeros(res.criticals_stored * 2 * nargs, dtype=np.float64)
             got = ctypes.c_uint64()
