@@ -392,6 +392,12 @@ template<unsigned P> inline MathExpr fixed_pow(const MathExpr& a) {
     return MathExpr(n);
 }
 inline MathExpr square(const MathExpr& a) { return fixed_pow<2>(a); }
+// literals (2_Z, 0.5_X) are expressions too
+inline MathExpr sqrt(const BoundedQ& a) { return sqrt(ensure_expr(a)); }
+inline MathExpr acos(const BoundedQ& a) { return acos(ensure_expr(a)); }
+inline MathExpr asin(const BoundedQ& a) { return asin(ensure_expr(a)); }
+inline MathExpr square(const BoundedQ& a) { return square(ensure_expr(a)); }
+template<unsigned P> inline MathExpr fixed_pow(const BoundedQ& a) { return fixed_pow<P>(ensure_expr(a)); }
 
 template<typename A1, typename... As,
          std::enable_if_t<sid_fe::IsExprLike<A1>::value, int> = 0>

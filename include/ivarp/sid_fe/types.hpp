@@ -6,6 +6,7 @@
 
 #include <chrono>
 #include <cmath>
+#include <limits>
 #include <cstddef>
 #include <cstdint>
 #include <exception>
@@ -42,13 +43,14 @@ private:
 using IFloat = Interval<float>;
 using IDouble = Interval<double>;
 
+/// "[lb, ub]" with the digits needed to read the endpoints back exactly, "~" in front when possibly
+/// undefined (the reference's float_interval_print.hpp:30-40).
 template<typename T> inline std::ostream& operator<<(std::ostream& o, const Interval<T>& i) {
+    const std::streamsize saved = o.precision(std::numeric_limits<T>::max_digits10);
     if(i.possibly_undefined()) o << '~';
-    o << '[';
-    if(i.finite_lb()) o << i.lb(); else o << "-inf";
-    o << ", ";
-    if(i.finite_ub()) o << i.ub(); else o << "inf";
-    return o << ']';
+    o << '[' << i.lb() << ", " << i.ub() << ']';
+    o.precision(saved);
+    return o;
 }
 
 /// Lexicographic order of intervals and boxes (used to sort reported criticals).
