@@ -111,15 +111,36 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def dist_setup():
+def dist_setup(backend="nccl"):
+    """One process per GPU under torchrun: (torch.distributed or None, rank, world size, local rank)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        dist.init_process_group(backend)
         return dist, rank, world, local
     return None, rank, world, local
+
+
+def shard_seed(rank):
+    """Each rank evaluates its own independent shard: the seeded batch of rank r uses SEED + r."""
+    return SEED + rank
+
+
+def max_over_ranks(dist, x, device="cuda"):
+    """The slowest rank's time (the whole job ends when it does); x unchanged without a process group."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Units all ranks processed per second of the slowest rank (weak scaling: fixed work per rank)."""
+    return units_per_rank * world / seconds
 
 
 def cpu_baseline(ir, lo, hi, threads, budget_s=1.5):
@@ -306,7 +327,7 @@ def run_ours(args):
     nargs = sid.ir_nargs(ir)
     lid = eng.register(ir)
     root = eng.root_box(lid, nargs)
-    lo, hi = sid.synthetic_batch(root, N_CUBOIDS, seed=SEED + rank)
+    lo, hi = sid.synthetic_batch(root, N_CUBOIDS, seed=shard_seed(rank))
     n = N_CUBOIDS
 
     # device-resident inputs and outputs
@@ -341,12 +362,10 @@ def run_ours(args):
     clk = clocks.stop()
     prof_calls, order_ms, eval_ms = eng.batch_profile_read()
     eng.batch_profile(False)
+    ms = max_over_ranks(dist, ms)
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
-    value = n * args.steps * world / (ms / 1000.0)
+    value = whole_job_rate(n * args.steps, world, ms / 1000.0)
 
     # end to end through the C ABI with pinned host buffers
     h_lo = torch.from_numpy(lo).pin_memory()
@@ -367,11 +386,8 @@ def run_ours(args):
     for _ in range(e2e_steps):
         e2e_step()
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = n * e2e_steps * world / e2e_s
+    e2e_s = max_over_ranks(dist, e2e_s)
+    e2e_value = whole_job_rate(n * e2e_steps, world, e2e_s)
     h2d = 2 * nargs * 8 * n
     d2h = 2 * nargs * 8 * n + n
 
