@@ -45,6 +45,9 @@ BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
 # (profiles/k_eval_batch_one_subcontainer_2e24.md); traffic grows in proportion to the batch
 NCU_TRAFFIC_BYTES_2E24 = 1.461791e9 + 1.385948e9
 NCU_FP64_PIPE_ACTIVE = 0.835
+# FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
+FP64_LANES_PER_CLOCK = 304
+OPS_TABLE = os.path.join(REPO, "tests", "golden", "ops_per_cuboid.json")
 # kernels of one sid_eval_batch_device call: ordering keys + histogram, two block scans, scan add, bucket
 # scatter, evaluation
 LAUNCHES_PER_EVAL = 6
@@ -429,6 +432,18 @@ def run_ours(args):
                   "criticals": best["criticals"], "seconds": best["seconds"],
                   "cuboids_per_s": best["cuboids"] / best["seconds"]},
     }
+    with open(OPS_TABLE) as f:
+        ops = json.load(f)["batch"][LEMMA]["total"]
+    sm_mhz = (clk.get("sm_max_mhz") or 2070.0)
+    peak_gops = FP64_LANES_PER_CLOCK * sm_mhz * 1e6 / 1e9
+    achieved_gops = ops * n / kernel_s / 1e9
+    line["roofline_fp64"] = {
+        "ops_per_cuboid": ops, "achieved": achieved_gops, "peak": peak_gops, "unit": "G IEEE ops/s",
+        "frac": achieved_gops / peak_gops, "pipe_active_ncu": NCU_FP64_PIPE_ACTIVE,
+        "note": "directed-rounding add/sub/mul/div/sqrt per cuboid from the op-counting oracle build "
+                "(tests/golden/ops_per_cuboid.json) over the evaluation kernel's time, against one FP64 "
+                "instruction per lane and clock; divisions, square roots, comparisons and selects cost more "
+                "FP64 instructions than they count here, hence the gap to the measured pipe activity"}
     if lemma_set:
         line["lemma_set"] = lemma_set
     if serve:

@@ -43,17 +43,27 @@ struct RoundDownScope {
     ~RoundDownScope() { std::fesetround(old); }
 };
 
+// Operation counting (the op-counting build, -DSIDO_COUNT_OPS, used to measure IEEE directed-rounding
+// operations per cuboid): additions/subtractions, multiplications, divisions, square roots, arc cosines.
+#ifdef SIDO_COUNT_OPS
+std::atomic<unsigned long long> g_ops[5];
+#define SIDO_COUNT(k) (g_ops[k].fetch_add(1, std::memory_order_relaxed))
+#else
+#define SIDO_COUNT(k) ((void)0)
+#endif
+
 // Directed basic operations; the ambient mode is round-down, upper bounds use the sign trick.
-template<class T> inline T add_rd(T a, T b) { return a + b; }
-template<class T> inline T add_ru(T a, T b) { return -((-a) - b); }
-template<class T> inline T sub_rd(T a, T b) { return a - b; }
-template<class T> inline T sub_ru(T a, T b) { return -(b - a); }
-template<class T> inline T mul_rd(T a, T b) { return a * b; }
-template<class T> inline T mul_ru(T a, T b) { return -((-a) * b); }
-template<class T> inline T div_rd(T a, T b) { return a / b; }
-template<class T> inline T div_ru(T a, T b) { return -((-a) / b); }
-template<class T> inline T sqrt_rd(T x) { return std::sqrt(x); }
+template<class T> inline T add_rd(T a, T b) { SIDO_COUNT(0); return a + b; }
+template<class T> inline T add_ru(T a, T b) { SIDO_COUNT(0); return -((-a) - b); }
+template<class T> inline T sub_rd(T a, T b) { SIDO_COUNT(0); return a - b; }
+template<class T> inline T sub_ru(T a, T b) { SIDO_COUNT(0); return -(b - a); }
+template<class T> inline T mul_rd(T a, T b) { SIDO_COUNT(1); return a * b; }
+template<class T> inline T mul_ru(T a, T b) { SIDO_COUNT(1); return -((-a) * b); }
+template<class T> inline T div_rd(T a, T b) { SIDO_COUNT(2); return a / b; }
+template<class T> inline T div_ru(T a, T b) { SIDO_COUNT(2); return -((-a) / b); }
+template<class T> inline T sqrt_rd(T x) { SIDO_COUNT(3); return std::sqrt(x); }
 template<class T> __attribute__((noinline)) T sqrt_ru(T x) {
+    SIDO_COUNT(3);
     std::fesetround(FE_UPWARD);
     volatile T vx = x;
     T r = std::sqrt(vx);
@@ -204,8 +214,10 @@ template<class T> struct Evaluator {
         T yl = even ? T(1) : lb, yu = even ? T(-1) : u;
         for(p /= 2; p > 0; p /= 2) {
             xl = xl * nxl; xu = xu * nxu;
+            SIDO_COUNT(1);
+            SIDO_COUNT(1);
             nxl = nl ? -xl : xl; nxu = nu ? -xu : xu;
-            if(p % 2) { yl = yl * nxl; yu = yu * nxu; }
+            if(p % 2) { yl = yl * nxl; yu = yu * nxu; SIDO_COUNT(1); SIDO_COUNT(1); }
         }
         return {yl, -yu, und};
     }
@@ -277,6 +289,8 @@ template<class T> struct Evaluator {
                 bool und = x.und;
                 if(CB(0).lb < -FX_ONE && x.lo < T(-1)) { und = true; x.lo = T(-1); }
                 if(CB(0).ub > FX_ONE && T(1) < x.hi) { und = true; x.hi = T(1); }
+                SIDO_COUNT(4);
+                SIDO_COUNT(4);
                 r = {acos_rounded<T>(x.hi, false), acos_rounded<T>(x.lo, true), und};
                 break;
             }
@@ -848,6 +862,14 @@ template<class T> void eval_operands_t(const LemmaIR& L, const std::vector<int>&
 }
 
 } // namespace
+
+void count_ops(unsigned long long out[5]) {
+#ifdef SIDO_COUNT_OPS
+    for(int k = 0; k < 5; ++k) out[k] = g_ops[k].exchange(0);
+#else
+    throw std::runtime_error("oracle: built without SIDO_COUNT_OPS");
+#endif
+}
 
 std::vector<int> operand_nodes(const std::string& ir) {
     return comparison_operands(sid::parse_lemma_ir(ir));

@@ -86,6 +86,10 @@ std::vector<int> operand_nodes(const std::string& ir);
 void eval_operands(const std::string& ir, const double* lo, const double* hi, std::uint64_t n, bool use_float,
                    double* out, std::int8_t* und, int threads);
 
+/// The op-counting build (-DSIDO_COUNT_OPS): IEEE directed-rounding operations executed since the last
+/// call (additions/subtractions, multiplications, divisions, square roots, arc cosines), then reset.
+void count_ops(unsigned long long out[5]);
+
 /// Initial runtime box (2*nargs doubles).
 std::vector<double> root_box(const std::string& ir);
 

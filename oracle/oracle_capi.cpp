@@ -96,6 +96,17 @@ int sido_eval_operands(const char* ir, const double* lo, const double* hi, unsig
     }
 }
 
+/* Op-counting build only: operations since the last call (add/sub, mul, div, sqrt, acos); 0 or -1. */
+int sido_count_ops(unsigned long long* out) {
+    try {
+        sido::count_ops(out);
+        return 0;
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
 /* acos(x) rounded down (up == 0) or up, for double (n doubles) and float (n floats); 0 or -1. */
 int sido_acos_rounded(const double* x, unsigned long long n, int up, double* out) {
     try {
