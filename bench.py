@@ -423,6 +423,10 @@ def run_ours(args):
         e2e_step()
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(dist, e2e_s)
+    torch.cuda.synchronize()
+    e2e_same = bool(np.array_equal(h_v.numpy(), o_v.cpu().numpy()) and
+                    np.array_equal(h_olo.numpy().view(np.uint64), o_lo.cpu().numpy().view(np.uint64)) and
+                    np.array_equal(h_ohi.numpy().view(np.uint64), o_hi.cpu().numpy().view(np.uint64)))
     e2e_value = whole_job_rate(n * e2e_steps, world, e2e_s)
     h2d = 2 * nargs * 8 * n
     d2h = 2 * nargs * 8 * n + n
@@ -453,7 +457,7 @@ def run_ours(args):
                    "batch_per_gpu": n, "parallelism": "independent shards per GPU (no collective)",
                    "l2": "inputs 805 MB and outputs exceed the 129 MB L2; no flush"},
         "e2e": {"value": e2e_value, "unit": "cuboids/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "outputs_equal_device_path": e2e_same},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC_BYTES_2E24 * n / float(1 << 24), "peak_kind": peak_kind,
                      "fp64_pipe_active_ncu": NCU_FP64_PIPE_ACTIVE,

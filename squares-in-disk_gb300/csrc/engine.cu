@@ -1494,9 +1494,24 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
         engine->batch_out_hi.reserve(cnt);
         engine->batch_verdict.reserve(std::size_t(n));
         // Pipeline in chunks: copies in on copy_in, ordering + evaluation on the engine stream, copies out on
-        // copy_out, so transfers of one chunk overlap the evaluation of its neighbours.
+        // copy_out, so transfers of one chunk overlap the evaluation of its neighbours. Nothing overlaps the
+        // copy-in of the first chunk or the copy-out of the last, so large batches start and end with
+        // chunks of 1/8, 1/8, 1/4, 1/2 of the steady-state size.
         const std::uint64_t chunk = kBatchChunk;
-        const std::uint64_t nchunks = (n + chunk - 1) / chunk;
+        std::vector<std::uint64_t> lens;
+        if(n >= 4 * chunk) {
+            const std::uint64_t ramp[4] = {chunk / 8, chunk / 8, chunk / 4, chunk / 2};
+            for(std::uint64_t r : ramp) lens.push_back(r);
+            for(std::uint64_t rest = n - 2 * chunk; rest > 0;) {
+                const std::uint64_t l = std::min(chunk, rest);
+                lens.push_back(l);
+                rest -= l;
+            }
+            for(int k = 3; k >= 0; --k) lens.push_back(ramp[k]);
+        } else {
+            for(std::uint64_t c0 = 0; c0 < n; c0 += chunk) lens.push_back(std::min(chunk, n - c0));
+        }
+        const std::size_t pitch = std::size_t(n) * sizeof(double);   // one row per variable
         std::vector<cudaEvent_t> evs;
         auto event = [&]() {
             cudaEvent_t e;
@@ -1505,15 +1520,13 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
             return e;
         };
         try {
-            for(std::uint64_t c = 0; c < nchunks; ++c) {
-                const std::uint64_t c0 = c * chunk, len = std::min(chunk, n - c0);
-                for(int v = 0; v < nargs; ++v) {
-                    const std::uint64_t off = std::uint64_t(v) * n + c0;
-                    cuda_check(cudaMemcpyAsync(engine->batch_in_lo.p + off, lo + off, len * sizeof(double),
-                                               cudaMemcpyHostToDevice, engine->copy_in), "H2D");
-                    cuda_check(cudaMemcpyAsync(engine->batch_in_hi.p + off, hi + off, len * sizeof(double),
-                                               cudaMemcpyHostToDevice, engine->copy_in), "H2D");
-                }
+            std::uint64_t c0 = 0;
+            for(const std::uint64_t len : lens) {
+                const std::size_t row = std::size_t(len) * sizeof(double);
+                cuda_check(cudaMemcpy2DAsync(engine->batch_in_lo.p + c0, pitch, lo + c0, pitch, row, std::size_t(nargs),
+                                             cudaMemcpyHostToDevice, engine->copy_in), "H2D");
+                cuda_check(cudaMemcpy2DAsync(engine->batch_in_hi.p + c0, pitch, hi + c0, pitch, row, std::size_t(nargs),
+                                             cudaMemcpyHostToDevice, engine->copy_in), "H2D");
                 cudaEvent_t in_done = event();
                 cuda_check(cudaEventRecord(in_done, engine->copy_in), "event record");
                 cuda_check(cudaStreamWaitEvent(engine->stream, in_done, 0), "stream wait");
@@ -1523,15 +1536,13 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
                 cudaEvent_t eval_done = event();
                 cuda_check(cudaEventRecord(eval_done, engine->stream), "event record");
                 cuda_check(cudaStreamWaitEvent(engine->copy_out, eval_done, 0), "stream wait");
-                for(int v = 0; v < nargs; ++v) {
-                    const std::uint64_t off = std::uint64_t(v) * n + c0;
-                    cuda_check(cudaMemcpyAsync(out_lo + off, engine->batch_out_lo.p + off, len * sizeof(double),
-                                               cudaMemcpyDeviceToHost, engine->copy_out), "D2H");
-                    cuda_check(cudaMemcpyAsync(out_hi + off, engine->batch_out_hi.p + off, len * sizeof(double),
-                                               cudaMemcpyDeviceToHost, engine->copy_out), "D2H");
-                }
+                cuda_check(cudaMemcpy2DAsync(out_lo + c0, pitch, engine->batch_out_lo.p + c0, pitch, row, std::size_t(nargs),
+                                             cudaMemcpyDeviceToHost, engine->copy_out), "D2H");
+                cuda_check(cudaMemcpy2DAsync(out_hi + c0, pitch, engine->batch_out_hi.p + c0, pitch, row, std::size_t(nargs),
+                                             cudaMemcpyDeviceToHost, engine->copy_out), "D2H");
                 cuda_check(cudaMemcpyAsync(verdict + c0, engine->batch_verdict.p + c0, std::size_t(len),
                                            cudaMemcpyDeviceToHost, engine->copy_out), "D2H");
+                c0 += len;
             }
             cuda_check(cudaStreamSynchronize(engine->copy_out), "eval batch sync");
         } catch(...) {

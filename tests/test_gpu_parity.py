@@ -58,6 +58,25 @@ def test_eval_batch_bit_exact(engine, oracle, name):
     assert len(np.unique(gv)) >= 2, "batch should exercise more than one verdict"
 
 
+@pytest.mark.parametrize("n", [(2 << 20) + 777, (4 << 20) + 4321])
+def test_host_batch_pipeline_equals_device_batch(engine, n):
+    """sid_eval_batch moves host buffers in chunks (uniform below 4 Mi cuboids, with short first and last chunks
+    above); every output must equal the device-resident single-call evaluation bit for bit."""
+    torch = pytest.importorskip("torch")
+    ir = sid.lemma_ir("one_subcontainer")
+    lid = engine.register(ir)
+    lo, hi = sid.synthetic_batch(engine.root_box(lid, sid.ir_nargs(ir)), n, seed=0x5EED0005)
+    hlo, hhi, hv = engine.eval_batch(lid, lo, hi)
+    d_lo, d_hi = torch.from_numpy(lo).cuda(), torch.from_numpy(hi).cuda()
+    o_lo, o_hi = torch.empty_like(d_lo), torch.empty_like(d_hi)
+    o_v = torch.empty(n, dtype=torch.int8, device="cuda")
+    engine.eval_batch_device(lid, d_lo.data_ptr(), d_hi.data_ptr(), n, o_lo.data_ptr(), o_hi.data_ptr(), o_v.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(hv, o_v.cpu().numpy())
+    assert np.array_equal(bits(hlo), bits(o_lo.cpu().numpy()))
+    assert np.array_equal(bits(hhi), bits(o_hi.cpu().numpy()))
+
+
 @pytest.mark.parametrize("variant", ["f64", "f32"])
 def test_expected_criticals_kat(engine, variant):
     ir = sid.lemma_ir("expected_critical_" + variant)
