@@ -66,4 +66,48 @@ template<class T> T acos_rounded(T x, bool up) {
     return up ? std::nextafter(rd, std::numeric_limits<T>::infinity()) : rd;
 }
 
+/// The float pass's arc cosine bound (lower for up = false, upper for up = true) as the device computes it
+/// for lemmas in double (squares-in-disk_gb300/csrc/acos.cuh, acos_bound_f32), restated: acos(x) = pi/2 -
+/// asin(x) for |x| <= 1/2, 2 asin(r) for x > 1/2, pi - 2 asin(r) for x < -1/2 with r = sqrt((1 - |x|)/2);
+/// asin(r) from the first 11 series terms with float coefficient bounds plus a remainder below r 2^-28.
+/// Runs in the oracle's ambient round-down mode; upper bounds as minus the lower bound of the negation.
+inline float acos_bound_f32(float x, bool up) {
+    static const float lo_c[11] = {0x1p+0f, 0x1.555554p-3f, 0x1.333332p-4f, 0x1.6db6dap-5f, 0x1.f1c71cp-6f,
+                                   0x1.6e8ba2p-6f, 0x1.1c4ec4p-6f, 0x1.c99998p-7f, 0x1.7a8786p-7f, 0x1.3fde50p-7f,
+                                   0x1.12ef3cp-7f};
+    static const float hi_c[11] = {0x1p+0f, 0x1.555556p-3f, 0x1.333334p-4f, 0x1.6db6dcp-5f, 0x1.f1c71ep-6f,
+                                   0x1.6e8ba4p-6f, 0x1.1c4ec6p-6f, 0x1.c9999ap-7f, 0x1.7a8788p-7f, 0x1.3fde52p-7f,
+                                   0x1.12ef3ep-7f};
+    if(!(x >= -1.0f && x <= 1.0f)) return acos_rounded<float>(x, up);
+    const bool negative = x < 0.0f;
+    const float a = negative ? -x : x;
+    const bool reduced = a > 0.5f;
+    // the bound of asin needed: upper exactly when the result's direction and the formula's sign differ
+    const bool want_upper = up != (reduced == negative);
+    float r = a;
+    if(reduced) {
+        r = std::sqrt((1.0f - a) * 0.5f);
+        if(want_upper) r = std::nextafter(r, std::numeric_limits<float>::infinity());
+    }
+    float r2, acc;
+    if(want_upper) {
+        r2 = -((-r) * r);
+        acc = -hi_c[10];
+        for(int k = 9; k >= 0; --k) acc = acc * r2 + (-hi_c[k]);
+        acc = acc * r;
+        acc = acc + (-r) * 0x1p-28f;
+    } else {
+        r2 = r * r;
+        acc = lo_c[10];
+        for(int k = 9; k >= 0; --k) acc = acc * r2 + lo_c[k];
+        acc = acc * r;
+    }
+    const float pi_lo = 0x1.921fb4p+1f, pi_hi = 0x1.921fb6p+1f;
+    float base;
+    if(reduced) base = negative ? (up ? -pi_hi : pi_lo) : 0.0f;
+    else base = up ? -pi_hi * 0.5f : pi_lo * 0.5f;
+    const float v = base + (reduced ? 2.0f * acc : acc);
+    return up ? -v : v;
+}
+
 } // namespace sido

@@ -89,7 +89,12 @@ template<class T> struct Evaluator {
     std::uint32_t epoch = 1;
     const Iv<T>* box = nullptr;
 
-    explicit Evaluator(const LemmaIR& l) : L(l), val(l.nodes.size()), pval(l.nodes.size()), stamp(l.nodes.size(), 0) {}
+    // the precision form's float pass of a lemma in double bounds acos with acos_bound_f32 instead of the
+    // correctly rounded float arc cosine
+    const bool fast_acos;
+
+    explicit Evaluator(const LemmaIR& l) : L(l), val(l.nodes.size()), pval(l.nodes.size()), stamp(l.nodes.size(), 0),
+        fast_acos(std::is_same<T, float>::value && l.numtype != "f32") {}
 
     void begin(const Iv<T>* b) {
         box = b;
@@ -291,7 +296,11 @@ template<class T> struct Evaluator {
                 if(CB(0).ub > FX_ONE && T(1) < x.hi) { und = true; x.hi = T(1); }
                 SIDO_COUNT(4);
                 SIDO_COUNT(4);
-                r = {acos_rounded<T>(x.hi, false), acos_rounded<T>(x.lo, true), und};
+                if(fast_acos) {
+                    r = {T(acos_bound_f32(float(x.hi), false)), T(acos_bound_f32(float(x.lo), true)), und};
+                } else {
+                    r = {acos_rounded<T>(x.hi, false), acos_rounded<T>(x.lo, true), und};
+                }
                 break;
             }
             case NodeOp::Ite: {

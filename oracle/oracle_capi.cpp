@@ -3,6 +3,7 @@
 #include "oracle.hpp"
 #include "acos_cr.hpp"
 
+#include <cfenv>
 #include <cstring>
 #include <exception>
 #include <string>
@@ -111,6 +112,20 @@ int sido_count_ops(unsigned long long* out) {
 int sido_acos_rounded(const double* x, unsigned long long n, int up, double* out) {
     try {
         for(unsigned long long i = 0; i < n; ++i) out[i] = sido::acos_rounded<double>(x[i], up != 0);
+        return 0;
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
+/// The float pass's arc cosine bound of lemmas in double (lower for up = 0), in the oracle's round-down mode.
+int sido_acos_bound_f32(const float* x, unsigned long long n, int up, float* out) {
+    try {
+        const int saved = std::fegetround();
+        std::fesetround(FE_DOWNWARD);
+        for(unsigned long long i = 0; i < n; ++i) out[i] = sido::acos_bound_f32(x[i], up != 0);
+        std::fesetround(saved);
         return 0;
     } catch(const std::exception& e) {
         last_error = e.what();

@@ -36,6 +36,8 @@ def lib():
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         _lib.sido_last_error.restype = ctypes.c_char_p
         _lib.sido_acos_rounded.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
+        _lib.sido_acos_rounded_f32.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
+        _lib.sido_acos_bound_f32.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
         _lib.sido_operand_nodes.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int]
         _lib.sido_eval_operands.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_ulonglong,
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
@@ -100,6 +102,15 @@ def acos_rounded(x, up, dtype=np.float64):
     out = np.empty_like(x)
     fn = lib().sido_acos_rounded if dtype == np.float64 else lib().sido_acos_rounded_f32
     if fn(x.ctypes.data, x.size, 1 if up else 0, out.ctypes.data) != 0:
+        raise RuntimeError(_err())
+    return out
+
+
+def acos_bound_f32(x, up):
+    """The precision form's float arc cosine bound (lower for up=False, upper for up=True) of every element."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty_like(x)
+    if lib().sido_acos_bound_f32(x.ctypes.data, x.size, 1 if up else 0, out.ctypes.data) != 0:
         raise RuntimeError(_err())
     return out
 

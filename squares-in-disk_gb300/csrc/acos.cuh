@@ -35,6 +35,7 @@
 // The same source compiles for the host (tests/acos_check.cpp checks it against 300-bit mpmath).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -436,6 +437,89 @@ SID_ACOS_HD inline float acos_ru(float x) {
     return float_of(static_cast<std::uint32_t>(acos_rounded_bits<24>(f32_to_f64_bits(float_bits(x)), true)));
 }
 
+// Rounding toward -inf for acos_bound_f32: the directed-rounding intrinsics on the device; on the host the
+// ambient rounding mode, which the caller must have set to FE_DOWNWARD (the CPU oracle runs in that mode).
+struct RoundDownF32 {
+    static SID_ACOS_HD inline float add(float a, float b) {
+#if defined(__CUDA_ARCH__)
+        return __fadd_rd(a, b);
+#else
+        return a + b;
+#endif
+    }
+    static SID_ACOS_HD inline float mul(float a, float b) {
+#if defined(__CUDA_ARCH__)
+        return __fmul_rd(a, b);
+#else
+        return a * b;
+#endif
+    }
+    static SID_ACOS_HD inline float sqrt(float a) {
+#if defined(__CUDA_ARCH__)
+        return __fsqrt_rd(a);
+#else
+        return std::sqrt(a);
+#endif
+    }
+};
+
+// Float bounds of the series coefficients c_k = binom(2k, k) / (4^k (2k + 1)) of asin(r) / r, k = 0..10,
+// rounded down (hi = false) and up (c_0 = 1 is exact); a function of a constant index, so that unrolled
+// device code sees immediates.
+SID_ACOS_HD constexpr float asin_coef(int k, bool hi) {
+    switch(k) {
+        case 0: return 0x1p+0f;
+        case 1: return hi ? 0x1.555556p-3f : 0x1.555554p-3f;
+        case 2: return hi ? 0x1.333334p-4f : 0x1.333332p-4f;
+        case 3: return hi ? 0x1.6db6dcp-5f : 0x1.6db6dap-5f;
+        case 4: return hi ? 0x1.f1c71ep-6f : 0x1.f1c71cp-6f;
+        case 5: return hi ? 0x1.6e8ba4p-6f : 0x1.6e8ba2p-6f;
+        case 6: return hi ? 0x1.1c4ec6p-6f : 0x1.1c4ec4p-6f;
+        case 7: return hi ? 0x1.c9999ap-7f : 0x1.c99998p-7f;
+        case 8: return hi ? 0x1.7a8788p-7f : 0x1.7a8786p-7f;
+        case 9: return hi ? 0x1.3fde52p-7f : 0x1.3fde50p-7f;
+        default: return hi ? 0x1.12ef3ep-7f : 0x1.12ef3cp-7f;
+    }
+}
+constexpr float kPiLoF = 0x1.921fb4p+1f, kPiHiF = 0x1.921fb6p+1f;
+constexpr float kHalfPiLoF = 0x1.921fb4p+0f, kHalfPiHiF = 0x1.921fb6p+0f;
+
+// A float bound of acos(x) for the precision form's float pass: lower (up = false) <= acos(x) <= upper
+// (up = true), a few float units wide, not correctly rounded (the float pass only has to enclose the
+// double evaluation, whose arc cosine is the correctly rounded one above).
+//   |x| <= 1/2: acos(x) = pi/2 - asin(x) (asin is odd); x > 1/2: 2 asin(r); x < -1/2: pi - 2 asin(r),
+//   r = sqrt((1 - |x|) / 2), where 1 - |x| and the halving are exact (Sterbenz);
+//   asin(r) = r * sum_{k <= 10} c_k r^(2k) + R with 0 <= R <= r c_11 4^-11 / (1 - 1/4) < r 2^-28 for
+//   0 <= r <= 1/2 (the c_k decrease).
+// Every operation rounds toward -inf; an upper bound is computed as minus the lower bound of the negated
+// quantity, so both directions run the same instructions on constants of the other rounding. The
+// successor of sqrt rounded down bounds the square root from above. Arguments outside [-1, 1] and NaN
+// give the correctly rounded function's result (NaN).
+template<class Op = RoundDownF32> SID_ACOS_HD inline float acos_bound_f32(float x, bool up) {
+    if(!(x >= -1.0f && x <= 1.0f)) return up ? acos_ru(x) : acos_rd(x);
+    const bool pos = x >= 0.0f;
+    const float ax = pos ? x : -x;
+    const bool big = ax > 0.5f;
+    const bool asin_up = up != (big != pos);       // which bound of asin the result needs
+    float r = ax;
+    if(big) {
+        r = Op::sqrt(Op::mul(Op::add(1.0f, -ax), 0.5f));
+        if(asin_up) r = float_of((float_bits(r) & 0x7fffffffu) + 1u);   // successor (1 - 1 is -0 rounding down)
+    }
+    // q: the lower bound of asin(r), or minus its upper bound
+    const float s = asin_up ? -Op::mul(-r, r) : Op::mul(r, r);
+    float q = asin_up ? -asin_coef(10, true) : asin_coef(10, false);
+    SID_ACOS_UNROLL
+    for(int k = 9; k >= 0; --k) q = Op::add(Op::mul(q, s), asin_up ? -asin_coef(k, true) : asin_coef(k, false));
+    q = Op::mul(q, r);
+    if(asin_up) q = Op::add(q, Op::mul(-r, 0x1p-28f));
+    float k0;
+    if(!up) k0 = big ? (pos ? 0.0f : kPiLoF) : kHalfPiLoF;
+    else k0 = big ? (pos ? 0.0f : -kPiHiF) : -kHalfPiHiF;
+    const float res = Op::add(k0, big ? Op::mul(2.0f, q) : q);
+    return up ? -res : res;
+}
+
 } // namespace acos_cr
 
 #if defined(__CUDACC__)
@@ -452,6 +536,26 @@ template<class T, bool CLAMP_LO, bool CLAMP_HI> __device__ inline Iv<T> iv_acos(
         x.hi = T(1);
     }
     return {acos_cr::acos_rd(x.hi), acos_cr::acos_ru(x.lo), und};
+}
+
+// Interval arc cosine of a lemma computed in double: double endpoints are the correctly rounded ones (the
+// plain form and the precision form's escalation), float endpoints (the precision form's float pass) the
+// cheaper enclosure acos_bound_f32.
+template<class T, bool CLAMP_LO, bool CLAMP_HI> __device__ inline Iv<T> iv_acos_f64(Iv<T> x) {
+    if constexpr(sizeof(T) == sizeof(double)) {
+        return iv_acos<T, CLAMP_LO, CLAMP_HI>(x);
+    } else {
+        bool und = x.und;
+        if(CLAMP_LO && x.lo < T(-1)) {
+            und = true;
+            x.lo = T(-1);
+        }
+        if(CLAMP_HI && T(1) < x.hi) {
+            und = true;
+            x.hi = T(1);
+        }
+        return {acos_cr::acos_bound_f32(x.hi, false), acos_cr::acos_bound_f32(x.lo, true), und};
+    }
 }
 #endif
 

@@ -197,7 +197,8 @@ class Emitter:
                     acc = "iv_%s(%s, %s)" % (op, x, acc)
                 rhs = acc
             elif op == "acos":
-                rhs = "iv_acos<T, %s, %s>(%s)" % ("true" if cn[0].lb < -FX_ONE else "false",
+                rhs = "%s<T, %s, %s>(%s)" % ("iv_acos" if self.L.numtype == "f32" else "iv_acos_f64",
+                                             "true" if cn[0].lb < -FX_ONE else "false",
                                                   "true" if cn[0].ub > FX_ONE else "false", ch[0])
             else:
                 raise ValueError("unsupported expression operation %s" % op)

@@ -468,8 +468,8 @@ template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(c
     if(t >= a.n) return;
     const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
     Iv<T> box[N];
-    #pragma unroll
     const std::uint64_t st = a.stride ? a.stride : a.n;
+    #pragma unroll
     for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
     std::int8_t vd = 0;
     if(propagate<L, T>(N - 1, box, N, 4)) vd = 1;

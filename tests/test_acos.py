@@ -190,3 +190,77 @@ def test_oracle_acos_correctly_rounded(oracle):
         assert (float(a), float(b)) == _expected(float(x), 24), x
     bad = oracle.acos_rounded(np.array([1.5, -1.0000000000000002, np.nan]), True)
     assert np.isnan(bad).all()
+
+
+# --- the precision form's float-pass bound (acos_bound_f32): sound, a few units wide, same bits in the oracle
+
+def build_bound_harness(out_dir, device=False):
+    """Compile tests/acos_bound_check.cpp for the host (g++, directed rounding by the FPU mode) or the GPU."""
+    exe = os.path.join(str(out_dir), "acos_bound_check_dev" if device else "acos_bound_check")
+    src = os.path.join(HERE, "acos_bound_check.cpp")
+    if device:
+        cmd = ["nvcc", "-std=c++17", "-O3", "-x", "cu", "-gencode", "arch=compute_103a,code=sm_103a", "--fmad=false",
+               "--ftz=false", "--prec-div=true", "--prec-sqrt=true", "-I", CSRC, src, "-o", exe]
+    else:
+        cmd = ["g++", "-std=c++17", "-O2", "-frounding-math", "-ffp-contract=off", "-I", CSRC, src, "-o", exe]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def bound_rows(exe, bits):
+    out = subprocess.run([exe], input="".join("%08x\n" % int(b) for b in bits), capture_output=True, text=True,
+                         check=True).stdout.split()
+    return np.array([int(v, 16) for v in out], dtype=np.uint32).reshape(-1, 4)
+
+
+def bound_sweep(exe, stride):
+    out = subprocess.run([exe, "sweep", str(stride)], capture_output=True, text=True, check=True).stdout.split()
+    checked, violations, _first, max_w, sum_w = (int(v) for v in out)
+    return checked, violations, max_w, sum_w / max(checked, 1)
+
+
+def bound_inputs():
+    """Float bit patterns: the branch boundaries +-1/2, +-1, signed zeros, subnormals, and seeded random floats."""
+    rng = np.random.default_rng(11)
+    edge = [0x3f000000, 0x3f000001, 0x3effffff, 0xbf000000, 0xbf000001, 0xbeffffff, 0x3f800000, 0xbf800000,
+            0x3f7fffff, 0xbf7fffff, 0, 0x80000000, 1, 0x80000001, 0x007fffff, 0x00800000, 0x3e800000]
+    rnd = list(rng.integers(0, 0x3f800001, 6000)) + list(0x80000000 | rng.integers(0, 0x3f800001, 6000))
+    return np.array(edge + rnd, dtype=np.uint32)
+
+
+@pytest.fixture(scope="module")
+def bound_harness(tmp_path_factory):
+    return build_bound_harness(tmp_path_factory.mktemp("acos_bound"))
+
+
+def test_acos_bound_coefficients_enclose_the_series(bound_harness):
+    """The float bounds of c_k = binom(2k, k) / (4^k (2k+1)) used by acos_bound_f32 are the neighbours of c_k,
+    and the remainder after 11 terms is below r 2^-28 for r <= 1/2."""
+    from fractions import Fraction
+    out = subprocess.run([bound_harness, "coef"], capture_output=True, text=True, check=True).stdout.split()
+    bounds = np.array([int(v, 16) for v in out], dtype=np.uint32).view(np.float32).reshape(11, 2)
+    for k in range(11):
+        c = Fraction(math.comb(2 * k, k), 4 ** k * (2 * k + 1))
+        f_lo, f_hi = bounds[k]
+        assert Fraction(float(f_lo)) <= c <= Fraction(float(f_hi)), k
+        assert f_lo == f_hi if Fraction(float(f_lo)) == c else np.nextafter(f_lo, np.float32(2)) == f_hi, k
+    c11 = Fraction(math.comb(22, 11), 4 ** 11 * 23)
+    assert c11 * Fraction(1, 4 ** 11) / Fraction(3, 4) < Fraction(1, 2 ** 28)
+
+
+def test_acos_bound_sound_on_a_strided_sweep_of_all_floats(bound_harness):
+    checked, violations, max_w, mean_w = bound_sweep(bound_harness, 4099)
+    assert checked > 500000 and violations == 0
+    assert max_w <= 8 and mean_w < 3.0
+
+
+def test_acos_bound_edges_and_oracle_restatement(bound_harness, oracle):
+    bits = bound_inputs()
+    rows = bound_rows(bound_harness, bits)
+    lo, hi, rd, ru = (rows[:, i].view(np.float32) for i in range(4))
+    assert (lo <= rd).all() and (hi >= ru).all()
+    x = bits.view(np.float32)
+    assert np.array_equal(oracle.acos_bound_f32(x, False).view(np.uint32), rows[:, 0])
+    assert np.array_equal(oracle.acos_bound_f32(x, True).view(np.uint32), rows[:, 1])
+    one = int(np.nonzero(bits == 0x3f800000)[0][0])
+    assert lo[one] == 0.0 and 0.0 < hi[one] < 1e-40    # acos(1) = 0 is enclosed by a subnormal upper end

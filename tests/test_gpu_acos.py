@@ -14,3 +14,21 @@ pytestmark = pytest.mark.gpu
 def test_device_acos_matches_golden_cases(tmp_path):
     exe = test_acos.build_harness(tmp_path, device=True)
     assert test_acos.check_golden(exe) > 1500
+
+
+def test_device_acos_bound_matches_host_build(tmp_path):
+    """The float pass's acos bound: the device build gives the host build's bits (same operations, directed
+    rounding by intrinsics instead of the FPU mode)."""
+    dev = test_acos.build_bound_harness(tmp_path, device=True)
+    host = test_acos.build_bound_harness(tmp_path, device=False)
+    bits = test_acos.bound_inputs()
+    assert (test_acos.bound_rows(dev, bits) == test_acos.bound_rows(host, bits)).all()
+
+
+def test_device_acos_bound_sound_on_a_sweep(tmp_path):
+    """Every 7th float of [-1, 1] (304 million arguments) on the device: lower <= acos rounded down and
+    upper >= acos rounded up, at most 8 units apart."""
+    dev = test_acos.build_bound_harness(tmp_path, device=True)
+    checked, violations, max_w, mean_w = test_acos.bound_sweep(dev, 7)
+    assert checked > 300_000_000 and violations == 0
+    assert max_w <= 8 and mean_w < 3.0

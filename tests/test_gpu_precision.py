@@ -40,6 +40,18 @@ def test_precision_form_matches_oracle(engine, oracle, name):
     assert g["escalated"] < g["cuboids"]
 
 
+def test_precision_form_acos_lemma_matches_oracle(engine, oracle):
+    """The float pass bounds acos with acos_bound_f32 (sound, not correctly rounded); the oracle restates it, so
+    the escalations of a lemma that uses acos (123 M cuboids; about a minute in the oracle) agree exactly."""
+    ir = sid.lemma_ir("more_subcontainers_2")
+    lid = engine.register(ir)
+    g = engine.prove(lid, precision=PRECISION_FP32)
+    o = oracle.prove(ir, fp32_first=True)
+    for k in ("cuboids", "leaves", "criticals", "escalated"):
+        assert g[k] == o[k], k
+    assert [g["cuboids"], g["leaves"]] == PUBLISHED["more_subcontainers_2"]
+
+
 @pytest.mark.parametrize("name", sid.lemma_names())
 def test_precision_form_proves_every_lemma(engine, name):
     lid = engine.register(sid.lemma_ir(name))
