@@ -92,6 +92,12 @@ typedef struct sid_prove_opts {
                                            checkpoint_every_steps steps and when stopping early */
     uint32_t checkpoint_every_steps;    /* 0: only when stopping early */
     uint32_t stop_after_steps;          /* > 0: stop after this many steps (with a checkpoint) */
+    uint32_t fp32_noprop_mask;          /* precision forms: float-pass levels that skip bound propagation and
+                                           test the rows on the child's float box (default none). Such a level
+                                           cannot refute a child that double keeps: the float box then contains
+                                           the double box before and after its propagation. Levels with a
+                                           split-invariant form evaluate the subexpressions that do not depend
+                                           on the split variable once per parent. */
 } sid_prove_opts;
 
 /* Fill `opts` with the defaults above. */
@@ -147,6 +153,7 @@ typedef struct sid_tuning {
     double level_escalation[SID_MAX_LEVELS];  /* measured escalation rate per level (-1: no children) */
     double seconds;                           /* proof time with the chosen configuration */
     double default_seconds;                   /* proof time with every level on the float pass, 65536 per step */
+    uint32_t fp32_noprop_mask;                /* float-pass levels without propagation (sid_prove_opts) */
 } sid_tuning;
 
 int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid_tuning* out);

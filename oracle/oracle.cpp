@@ -575,7 +575,9 @@ template<class T> struct Driver {
             const float hi = (i + 1 >= n) ? ub_hi : -((-lb_hi) - (-(-float(i + 1) * w_hi)));
             fb[std::size_t(arg)] = {lo, hi, false};
         }
-        bool refuted = S.F->propagate(arg, fb.data(), it, rec) || (r1 > r0 && !S.F->rows_ok(r0, r1, fb.data()));
+        const bool noprop = level < 32 && ((opt.fp32_noprop_mask >> level) & 1u);
+        bool refuted = (!noprop && S.F->propagate(arg, fb.data(), it, rec)) ||
+                       (r1 > r0 && !S.F->rows_ok(r0, r1, fb.data()));
         if(refuted) ++c.fp32_refuted; else ++c.escalated;
         return refuted;
     }

@@ -9,7 +9,11 @@ For every lemma IR file (written by the front end, include/ivarp/sid_fe/compile.
     evaluated only when needed, like the reference's if_then_else evaluation);
   * rows_ok<T>(r0, r1, box): do all constraints of rows [r0, r1) possibly hold (stops at the first
     violated constraint, like CPUProverCore::p_cuboid_violates_constraint_row);
-  * the update lists as 64-bit masks, the targets and the compile-time variable bounds.
+  * the update lists as 64-bit masks, the targets and the compile-time variable bounds;
+  * for double lemmas, per level that tests rows, the split-invariant form of the precision form's float
+    pass (H<level>): prelude() evaluates once per parent every row subexpression that does not depend on
+    the level's split variable and stores the ones the other subexpressions consume; child() evaluates
+    the rest per child from those values.
 
 Interval operations whose case analysis depends on compile-time bounds get those decisions as
 template arguments (see interval.cuh). The code is generic in the number type T so the same lemma
@@ -258,6 +262,139 @@ class Emitter:
         return name
 
 
+def levels_with_rows(L):
+    """(level id, split variable, r0, r1) of the levels that test constraint rows [r0, r1): the last dynamic
+    level tests the last row, static level j the rows from its variable up to the next static variable.
+    Level ids: dynamic levels 0..D-1, then static levels D + j."""
+    dyn = [s for s in L.splits if s[3]]
+    stat = [s for s in L.splits if not s[3]]
+    out = []
+    if dyn:
+        out.append((len(dyn) - 1, dyn[-1][0], L.nargs - 1, L.nargs))
+    for j, sp in enumerate(stat):
+        r1 = stat[j + 1][0] if j + 1 < len(stat) else L.nargs
+        if r1 > sp[0]:
+            out.append((len(dyn) + j, sp[0], sp[0], r1))
+    return out
+
+
+HOIST_BITS = 63   # flag bits per parent (bit 63 marks a parent whose split-invariant constraints already fail)
+
+
+def hoist_plan(L, var, r0, r1):
+    """Split the rows [r0, r1) for a split of `var`: constraints independent of var (tested once per parent),
+    constraints that depend on it (tested per child), and the frontier: nodes independent of var that
+    var-dependent nodes consume (stored per parent). None if the frontier's flags do not fit the flag word."""
+    memo = {}
+
+    def deps(nid):
+        if nid not in memo:
+            n = L.nodes[nid]
+            d = {n.aux} if n.op == "arg" else set()
+            for c in n.ch:
+                d |= deps(c)
+            memo[nid] = frozenset(d)
+        return memo[nid]
+
+    top = [L.constraints[ci] for r in range(r0, r1) for ci in L.rows.get(r, [])]
+    if not top:
+        return None
+    inv_top = [p for p in top if var not in deps(p)]
+    dep_top = [p for p in top if var in deps(p)]
+    frontier, seen, fset = [], set(), set()
+
+    def walk(x):
+        if x in seen:
+            return
+        seen.add(x)
+        for c in L.nodes[x].ch:
+            cn = L.nodes[c]
+            if var in deps(c):
+                walk(c)
+            elif cn.op in ("arg", "const", "bconst") or (cn.op in PRED_OPS and cn.lb == cn.ub):
+                continue
+            elif c not in fset:
+                fset.add(c)
+                frontier.append(c)
+
+    for p in dep_top:
+        walk(p)
+    bits = sum(2 if L.nodes[f].op in PRED_OPS else 1 for f in frontier)
+    if bits > HOIST_BITS:
+        return None
+    return inv_top, dep_top, frontier
+
+
+def emit_hoisted(L, level, var, plan, w):
+    """H<level>: prelude (once per parent: split-invariant constraints, stored frontier values and flags) and
+    child (per child: the constraints that depend on the split variable)."""
+    inv_top, dep_top, frontier = plan
+    slots, bit = {}, 0
+    nval = 0
+    for f in frontier:
+        if L.nodes[f].op in PRED_OPS:
+            slots[f] = ("p", bit)
+            bit += 2
+        else:
+            slots[f] = ("v", nval, bit)
+            nval += 1
+            bit += 1
+    w("template<> struct H<%d> {" % level)
+    w("    static constexpr int VAR = %d;" % var)
+    w("    static constexpr int NVAL = %d;" % nval)
+    w("    __device__ static bool prelude(const Iv<float>* box, float2* hv, std::uint64_t stride, std::uint64_t j,")
+    w("                                   std::uint64_t& bits) {")
+    w("        using T = float;")
+    w("        std::uint64_t b = 0;")
+    e = Emitter(L)
+    e.indent = 2
+    scope = {}
+    for p in inv_top:
+        x = e.pred(p, scope)
+        e.emit("if(!%s.ub) return false;" % x)
+    for f in frontier:
+        sl = slots[f]
+        if sl[0] == "p":
+            x = e.pred(f, scope)
+            e.emit("if(%s.lb) b |= 0x%xull;" % (x, 1 << sl[1]))
+            e.emit("if(%s.ub) b |= 0x%xull;" % (x, 1 << (sl[1] + 1)))
+        else:
+            x = e.expr(f, scope)
+            e.emit("hv[%d * stride + j] = make_float2(%s.lo, %s.hi);" % (sl[1], x, x))
+            e.emit("if(%s.und) b |= 0x%xull;" % (x, 1 << sl[2]))
+    w("\n".join(e.lines))
+    w("        (void)box; (void)hv; (void)stride; (void)j;")
+    w("        bits = b;")
+    w("        return true;")
+    w("    }")
+    w("    __device__ static bool child(const Iv<float>* box, const float2* hv, std::uint64_t stride, std::uint64_t j,")
+    w("                                 std::uint64_t bits) {")
+    w("        using T = float;")
+    e = Emitter(L)
+    e.indent = 2
+    scope = {}
+    for f in frontier:
+        sl = slots[f]
+        if sl[0] == "p":
+            name = "q%d" % f
+            e.emit("const IB %s{(bits & 0x%xull) != 0, (bits & 0x%xull) != 0};" % (name, 1 << sl[1], 1 << (sl[1] + 1)))
+        else:
+            name = "h%d" % f
+            e.emit("const float2 %s_ = hv[%d * stride + j];" % (name, sl[1]))
+            e.emit("const Iv<T> %s{%s_.x, %s_.y, (bits & 0x%xull) != 0};" % (name, name, name, 1 << sl[2]))
+        scope[f] = name
+    for p in dep_top:
+        x = e.pred(p, scope)
+        e.emit("if(!%s.ub) return false;" % x)
+    w("\n".join(e.lines))
+    w("        (void)box; (void)hv; (void)stride; (void)j; (void)bits;")
+    w("        return true;")
+    w("    }")
+    w("};")
+    w("")
+    return nval
+
+
 def mask(ids):
     m = 0
     for i in ids:
@@ -352,6 +489,37 @@ def generate(lemma):
     w("    return true;")
     w("}")
     w("")
+    hoisted = []
+    if L.numtype != "f32":
+        w("template<int LV> struct H;")
+        w("")
+        for level, var, r0, r1 in levels_with_rows(L):
+            plan = hoist_plan(L, var, r0, r1)
+            if plan is not None:
+                hoisted.append((level, emit_hoisted(L, level, var, plan, w)))
+        w("static int hoist_values(int lv) {")
+        w("    switch(lv) {")
+        for level, nval in hoisted:
+            w("        case %d: return %d;" % (level, nval))
+        w("        default: return -1;")
+        w("    }")
+        w("}")
+        w("static cudaError_t prelude_f32(int lv, const LevelArgs& a, std::uint64_t n_items, float2* hv, std::uint64_t* hb,")
+        w("                               cudaStream_t s) {")
+        w("    switch(lv) {")
+        for level, _ in hoisted:
+            w("        case %d: return launch_prelude_f32<L, H<%d>>(a, n_items, hv, hb, s);" % (level, level))
+        w("        default: return cudaErrorInvalidValue;")
+        w("    }")
+        w("}")
+        w("static cudaError_t filter_hoisted(int lv, const LevelArgs& a, cudaStream_t s) {")
+        w("    switch(lv) {")
+        for level, _ in hoisted:
+            w("        case %d: return launch_filter_hoisted<L, H<%d>>(a, s);" % (level, level))
+        w("        default: return cudaErrorInvalidValue;")
+        w("    }")
+        w("}")
+        w("")
     w("static cudaError_t level(int mode, const LevelArgs& a, cudaStream_t s) { return launch_level<L, %s>(mode, a, s); }" % T_plain)
     w("static cudaError_t root_box(double2* o, cudaStream_t s) { return launch_root_box<L, %s>(o, s); }" % T_plain)
     w("static cudaError_t eval_batch(const BatchArgs& a, cudaStream_t s) { return launch_eval_batch<L, %s>(a, s); }" % T_plain)
@@ -364,7 +532,8 @@ def generate(lemma):
     w("} // namespace %s" % ns)
     w("")
     w("extern const LemmaKernels kernels_%s;" % ns)
-    prec = "nullptr, nullptr" if L.numtype == "f32" else "&%s::filter_f32, &%s::level_esc" % (ns, ns)
+    prec = ("nullptr, nullptr, nullptr, nullptr, nullptr" if L.numtype == "f32" else
+            "&{0}::filter_f32, &{0}::level_esc, &{0}::hoist_values, &{0}::prelude_f32, &{0}::filter_hoisted".format(ns))
     w("const LemmaKernels kernels_%s = {\"%s\", 0x%016xull, %d, %d, %s, &%s::level, &%s::root_box, &%s::eval_batch, %s};" % (
         ns, L.slug, L.fingerprint, L.nargs, len(L.bounds), "true" if L.numtype == "f32" else "false", ns, ns, ns, prec))
     w("")

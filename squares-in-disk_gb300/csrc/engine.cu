@@ -209,6 +209,7 @@ namespace sid {
 constexpr std::uint64_t kLevelCapItems = std::uint64_t(8) << 20;   // items per intermediate level list
 constexpr std::uint64_t kDefaultStep = std::uint64_t(1) << 16;     // queue elements per step
 constexpr std::uint64_t kEscChunk = std::uint64_t(1) << 24;        // children per precision-form pass pair
+constexpr std::uint64_t kHoistBytes = std::uint64_t(256) << 20;     // split-invariant values of one chunk's parents
 constexpr unsigned kEscBlocksPerSM = 8;                            // grid of the escalated (double) pass
 constexpr int kDefaultSlots = 1024;
 
@@ -424,6 +425,7 @@ struct Lane {
     std::uint64_t step_cap = kDefaultStep;
     bool fp32_first = false;
     std::uint32_t fp32_mask = ~0u;         // levels (dynamic d, static D + j) that use the float pass
+    std::uint32_t noprop_mask = 0;         // float-pass levels without bound propagation (split-invariant form)
     std::uint64_t fanout = 1, root_fanout = 1;
     int sm_count = 1;
     int max_slots = kDefaultSlots;
@@ -438,6 +440,8 @@ struct Lane {
     DevBuf<std::uint32_t> esc;
     DevBuf<float2> pbox;                  // precision form: per-parent float boxes of one chunk
     DevBuf<float4> psplit;
+    DevBuf<float2> hval;                  // split-invariant float pass: stored values per parent of one chunk
+    DevBuf<std::uint64_t> hbits;
     DevBuf<GatherEntry> gather;
     std::vector<GatherEntry> gather_host;
     long long grown_bytes = 0;             // device bytes request queues grew by since the last take_grown_bytes
@@ -468,10 +472,11 @@ struct Lane {
         if(own_stream && st) cudaStreamDestroy(st);
     }
 
-    void configure(std::uint64_t step_elements, bool fp32, std::uint32_t mask = ~0u) {
+    void configure(std::uint64_t step_elements, bool fp32, std::uint32_t mask = ~0u, std::uint32_t noprop = 0) {
         step_cap = step_elements > 0 ? step_elements : kDefaultStep;
         fp32_first = fp32 && lem->k->filter_f32 != nullptr;
         fp32_mask = mask;
+        noprop_mask = noprop;
         level_esc.reserve(SID_MAX_LEVELS);
         cuda_check(cudaMemsetAsync(level_esc.p, 0, SID_MAX_LEVELS * sizeof(unsigned long long), st), "level stats");
         level_children.assign(SID_MAX_LEVELS, 0);
@@ -681,12 +686,21 @@ struct Lane {
             return;
         }
         // precision form: per-parent float data, float pass over a chunk of children, then double pass over
-        // the chunk's escalation list
-        for(std::uint64_t cb = 0; cb < total; cb += kEscChunk) {
+        // the chunk's escalation list. Without propagation, where the lemma has a split-invariant form of the
+        // level, the float pass runs in two kernels: once per parent (k_prelude_f32), then per child.
+        const bool noprop = ((noprop_mask >> level) & 1u) != 0;
+        const int nval = noprop && lem->k->hoist_values ? lem->k->hoist_values(level) : -1;
+        std::uint64_t chunk = kEscChunk;
+        if(nval > 0) {   // keep the stored values of a chunk's parents within kHoistBytes
+            const std::uint64_t parents = std::max<std::uint64_t>(1, kHoistBytes / (sizeof(float2) * std::uint64_t(nval)));
+            chunk = std::min(kEscChunk, std::max<std::uint64_t>(1, parents - 1) * std::uint64_t(a0.nsub));
+        }
+        for(std::uint64_t cb = 0; cb < total; cb += chunk) {
             LevelArgs a = a0;
             a.count_cuboids = false;
+            a.fp32_noprop = noprop;
             a.child_begin = cb;
-            a.n_child = std::min(kEscChunk, total - cb);
+            a.n_child = std::min(chunk, total - cb);
             a.esc = esc.p;
             a.esc_count = counters.p + 3;
             const std::uint64_t nsub = std::uint64_t(a.nsub);
@@ -702,7 +716,16 @@ struct Lane {
             a.pstride = n_items;
             a.pitem_begin = first;
             cuda_check(cudaMemsetAsync(a.esc_count, 0, sizeof(unsigned long long), st), "reset escalation count");
-            cuda_check(lem->k->filter_f32(a, st), "float pass launch");
+            if(nval >= 0) {
+                hval.reserve(std::size_t(std::max(nval, 1)) * n_items);
+                hbits.reserve(n_items);
+                cuda_check(lem->k->prelude_f32(level, a, n_items, hval.p, hbits.p, st), "parent float pass launch");
+                a.hval = hval.p;
+                a.hbits = hbits.p;
+                cuda_check(lem->k->filter_hoisted(level, a, st), "float pass launch");
+            } else {
+                cuda_check(lem->k->filter_f32(a, st), "float pass launch");
+            }
             k_add_counter<<<1, 1, 0, st>>>(level_esc.p + level, a.esc_count);
             const std::uint64_t want = (a.n_child + 127) / 128;
             const unsigned blocks = unsigned(std::min<std::uint64_t>(want, std::uint64_t(sm_count) * kEscBlocksPerSM));
@@ -1059,7 +1082,8 @@ void read_checkpoint(const char* path, ProofState& ps) {
 /// step/mask override the step size and the float-pass levels (autotuning); `resume` continues from a
 /// checkpoint.
 void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_result* res, std::uint64_t step_override = 0,
-               const std::uint32_t* mask_override = nullptr, const ProofState* resume = nullptr) {
+               const std::uint32_t* mask_override = nullptr, const ProofState* resume = nullptr,
+               const std::uint32_t* noprop_override = nullptr) {
     Lemma* lem = get_lemma(eng, lemma_id);
     if(o.max_iterations_per_node > 1) {
         fail(SID_ERR_UNSUPPORTED, "max_iterations_per_node > 1 (re-iteration of a node) is not supported; use 1");
@@ -1071,7 +1095,8 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
     const std::uint64_t step = o.batch_elements > 0 ? std::uint64_t(o.batch_elements)
                                                     : (tuned ? std::uint64_t(lem->tuning.step_elements) : kDefaultStep);
     lane.configure(step_override ? step_override : step, o.precision != SID_PRECISION_PLAIN,
-                   mask_override ? *mask_override : (tuned ? lem->tuning.fp32_level_mask : o.fp32_level_mask));
+                   mask_override ? *mask_override : (tuned ? lem->tuning.fp32_level_mask : o.fp32_level_mask),
+                   noprop_override ? *noprop_override : (tuned ? lem->tuning.fp32_noprop_mask : o.fp32_noprop_mask));
 
     Request r;
     r.lem = lem;
@@ -1216,7 +1241,8 @@ struct sid_server {
             const bool tuned = opts.precision == SID_PRECISION_FP32_TUNED && lem->tuned;
             w->lane->configure(opts.step_elements > 0 ? std::uint64_t(opts.step_elements)
                                                       : (tuned ? std::uint64_t(lem->tuning.step_elements) : kDefaultStep),
-                               opts.precision != SID_PRECISION_PLAIN, tuned ? lem->tuning.fp32_level_mask : ~0u);
+                               opts.precision != SID_PRECISION_PLAIN, tuned ? lem->tuning.fp32_level_mask : ~0u,
+                               tuned ? lem->tuning.fp32_noprop_mask : 0u);
             Lane& lane = *w->lane;
             for(;;) {
                 std::vector<Request*> admit;
@@ -1332,6 +1358,7 @@ void sid_prove_opts_default(sid_prove_opts* o) {
     o->progress_first_ms = 8000;
     o->progress_every_ms = 2000;
     o->fp32_level_mask = ~0u;
+    o->fp32_noprop_mask = 0;
 }
 
 const char* sid_last_error(void) { return g_last_error; }
@@ -1573,10 +1600,11 @@ int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid
         o.precision = SID_PRECISION_FP32_ESCALATE;
         o.max_criticals_kept = 0;
         double spent = 0;
+        std::uint32_t noprop = 0;
         auto timed = [&](std::uint64_t step, std::uint32_t mask, sid_result& best) {
             for(int rep = 0; rep < 2; ++rep) {
                 sid_result r{};
-                prove_one(engine, lemma_id, o, &r, step, &mask);
+                prove_one(engine, lemma_id, o, &r, step, &mask, nullptr, &noprop);
                 spent += r.seconds;
                 if(rep == 0 || r.seconds < best.seconds) best = r;
             }
@@ -1621,6 +1649,25 @@ int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid
                     t.escalation_threshold = cand.first;
                 }
             }
+            // float passes without propagation, in the split-invariant form: on every level that has one, or
+            // only on the innermost static level
+            std::uint32_t hoistable = 0;
+            for(int k = 0; k < std::min(levels, SID_MAX_LEVELS); ++k) {
+                if(l->k->hoist_values && l->k->hoist_values(k) >= 0) hoistable |= 1u << k;
+            }
+            const std::uint32_t innermost = levels > 0 ? 1u << std::min(levels - 1, SID_MAX_LEVELS - 1) : 0u;
+            for(std::uint32_t cand : {hoistable & t.fp32_level_mask, hoistable & innermost & t.fp32_level_mask}) {
+                if(spent > max_seconds || cand == 0 || cand == t.fp32_noprop_mask) continue;
+                sid_result r{};
+                noprop = cand;
+                timed(kDefaultStep, t.fp32_level_mask, r);
+                ++t.candidates;
+                if(same(r) && r.seconds < t.seconds) {
+                    t.seconds = r.seconds;
+                    t.fp32_noprop_mask = cand;
+                }
+            }
+            noprop = t.fp32_noprop_mask;
             for(std::uint64_t step : {std::uint64_t(1) << 15, std::uint64_t(1) << 17, std::uint64_t(1) << 14}) {
                 if(spent > max_seconds) break;
                 sid_result r{};

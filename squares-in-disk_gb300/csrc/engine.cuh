@@ -209,6 +209,11 @@ struct LevelArgs {
     const float2* pbox;               // pbox[v*pstride + j]; for the split variable (RD(lb), RU(ub))
     const float4* psplit;             // (RD(w), RU(lb), RU(w), 0) with w the double split width
     std::uint64_t pstride, pitem_begin;
+    bool fp32_noprop;                 // float pass without bound propagation (rows only)
+    // split-invariant float pass (k_prelude_f32 / k_filter_hoisted): per parent j, stored subexpression
+    // values hval[k*pstride + j] and their flags hbits[j] (kParentRefuted: no child can satisfy the rows)
+    const float2* hval;
+    const std::uint64_t* hbits;
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -379,6 +384,19 @@ __device__ __forceinline__ void split_child_f32(float lb_lo, float ub_hi, float4
 #ifndef SID_FILTER_MIN_BLOCKS
 #define SID_FILTER_MIN_BLOCKS 8     // resident 128-thread blocks per SM the float pass is compiled for (64 registers)
 #endif
+/// End of a float-pass child: undecided children (ok) are appended to the escalation list (warp ballot),
+/// refuted ones count as leaves; every child counts as a cuboid of its request.
+__device__ __forceinline__ void filter_result(const LevelArgs& a, unsigned active, std::uint64_t item, std::uint64_t t,
+                                              bool ok) {
+    const unsigned m = __ballot_sync(active, ok);
+    const int leader = __ffs(active) - 1;
+    unsigned long long base = 0;
+    if(int(lane_id()) == leader && m) base = atomicAdd(a.esc_count, (unsigned long long)__popc(m));
+    base = __shfl_sync(active, base, leader);
+    if(ok) a.esc[base + __popc(m & lanes_below())] = std::uint32_t(t);
+    add_to_requests<RC_CUBOIDS, RC_LEAVES, RC_ESCALATED>(active, a.req, item_tag(a, item), 1u, ok ? 0u : 1u, ok ? 1u : 0u);
+}
+
 template<class L> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) k_filter_f32(const LevelArgs a) {
     constexpr int N = L::NARGS;
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -395,15 +413,56 @@ template<class L> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) 
         box[v] = {f.x, f.y, false};
         if(v == a.var) split_child_f32(f.x, f.y, a.psplit[j], a.nsub, c, box[v].lo, box[v].hi);
     }
-    bool ok = !propagate<L, float>(a.var, box, a.it_limit, a.rec_limit);
+    bool ok = a.fp32_noprop || !propagate<L, float>(a.var, box, a.it_limit, a.rec_limit);
     if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<float>(a.row_begin, a.row_end, box);
-    const unsigned m = __ballot_sync(active, ok);
-    const int leader = __ffs(active) - 1;
-    unsigned long long base = 0;
-    if(int(lane_id()) == leader && m) base = atomicAdd(a.esc_count, (unsigned long long)__popc(m));
-    base = __shfl_sync(active, base, leader);
-    if(ok) a.esc[base + __popc(m & lanes_below())] = std::uint32_t(t);
-    add_to_requests<RC_CUBOIDS, RC_LEAVES, RC_ESCALATED>(active, a.req, item_tag(a, item), 1u, ok ? 0u : 1u, ok ? 1u : 0u);
+    filter_result(a, active, item, t, ok);
+}
+
+constexpr std::uint64_t kParentRefuted = 1ull << 63;
+
+/// Split-invariant float pass, per parent: without propagation a child's float box differs from its
+/// parent's only in the split variable, so every row subexpression that does not depend on it has one
+/// value per parent. H::prelude tests the constraints that do not depend on the split variable (if one
+/// fails, no child can pass: kParentRefuted) and stores the values the other constraints consume.
+template<class L, class H> __global__ void __launch_bounds__(128) k_prelude_f32(const LevelArgs a, std::uint64_t n_items,
+                                                                                 float2* hval, std::uint64_t* hbits) {
+    constexpr int N = L::NARGS;
+    const std::uint64_t j = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(j >= n_items) return;
+    Iv<float> box[N];
+    #pragma unroll
+    for(int v = 0; v < N; ++v) {
+        const float2 f = a.pbox[std::uint64_t(v) * a.pstride + j];
+        box[v] = {f.x, f.y, false};
+    }
+    std::uint64_t bits = 0;
+    hbits[j] = H::prelude(box, hval, a.pstride, j, bits) ? bits : kParentRefuted;
+}
+
+/// Split-invariant float pass, per child: the constraints that depend on the split variable, from the
+/// parent's stored values. Decides exactly as rows_ok on the child's float box without propagation.
+template<class L, class H> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) k_filter_hoisted(const LevelArgs a) {
+    constexpr int N = L::NARGS;
+    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(t >= a.n_child) return;
+    const unsigned active = __activemask();
+    const std::uint64_t id = a.child_begin + t;
+    const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
+    const std::uint64_t j = id / std::uint64_t(a.nsub) - a.pitem_begin;
+    const int c = int(id % std::uint64_t(a.nsub));
+    const std::uint64_t bits = a.hbits[j];
+    bool ok = (bits & kParentRefuted) == 0;
+    if(ok) {
+        Iv<float> box[N];
+        #pragma unroll
+        for(int v = 0; v < N; ++v) {
+            const float2 f = a.pbox[std::uint64_t(v) * a.pstride + j];
+            box[v] = {f.x, f.y, false};
+            if(v == H::VAR) split_child_f32(f.x, f.y, a.psplit[j], a.nsub, c, box[v].lo, box[v].hi);
+        }
+        ok = H::child(box, a.hval, a.pstride, j, bits);
+    }
+    filter_result(a, active, item, t, ok);
 }
 
 /// Precision form, second pass: the escalated children, in double, with the plain form's outputs.
@@ -495,6 +554,12 @@ struct LemmaKernels {
     // precision form (double lemmas only; null for float lemmas)
     cudaError_t (*filter_f32)(const LevelArgs& a, cudaStream_t s);
     cudaError_t (*level_esc)(int mode, const LevelArgs& a, unsigned blocks, cudaStream_t s);
+    // split-invariant float pass per level id (dynamic d, static D + j): stored values per parent, -1 where
+    // the level has no such form (no rows, or too many stored values)
+    int (*hoist_values)(int level);
+    cudaError_t (*prelude_f32)(int level, const LevelArgs& a, std::uint64_t n_items, float2* hval, std::uint64_t* hbits,
+                               cudaStream_t s);
+    cudaError_t (*filter_hoisted)(int level, const LevelArgs& a, cudaStream_t s);
 };
 
 template<class L, class T> cudaError_t launch_level(int mode, const LevelArgs& a, cudaStream_t s) {
@@ -518,6 +583,24 @@ template<class L> cudaError_t launch_filter_f32(const LevelArgs& a, cudaStream_t
     const std::uint64_t blocks = (a.n_child + 127) / 128;
     if(blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     k_filter_f32<L><<<unsigned(blocks), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template<class L, class H> cudaError_t launch_prelude_f32(const LevelArgs& a, std::uint64_t n_items, float2* hval,
+                                                          std::uint64_t* hbits, cudaStream_t s) {
+    if(n_items == 0) return cudaSuccess;
+    const std::uint64_t blocks = (n_items + 127) / 128;
+    if(blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    k_prelude_f32<L, H><<<unsigned(blocks), 128, 0, s>>>(a, n_items, hval, hbits);
+    return cudaGetLastError();
+}
+
+template<class L, class H> cudaError_t launch_filter_hoisted(const LevelArgs& a, cudaStream_t s) {
+    if(a.n_child == 0) return cudaSuccess;
+    if(a.var != H::VAR) return cudaErrorInvalidValue;
+    const std::uint64_t blocks = (a.n_child + 127) / 128;
+    if(blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    k_filter_hoisted<L, H><<<unsigned(blocks), 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -50,7 +50,7 @@ class SidProveOpts(ctypes.Structure):
                 ("progress_user", ctypes.c_void_p), ("progress_first_ms", ctypes.c_uint32),
                 ("progress_every_ms", ctypes.c_uint32), ("fp32_level_mask", ctypes.c_uint32),
                 ("checkpoint_path", ctypes.c_char_p), ("checkpoint_every_steps", ctypes.c_uint32),
-                ("stop_after_steps", ctypes.c_uint32)]
+                ("stop_after_steps", ctypes.c_uint32), ("fp32_noprop_mask", ctypes.c_uint32)]
 
 
 class SidServerOpts(ctypes.Structure):
@@ -76,7 +76,7 @@ class SidTuning(ctypes.Structure):
     _fields_ = [("step_elements", ctypes.c_int64), ("fp32_level_mask", ctypes.c_uint32),
                 ("escalation_threshold", ctypes.c_float), ("levels", ctypes.c_int32), ("candidates", ctypes.c_uint32),
                 ("level_escalation", ctypes.c_double * MAX_LEVELS), ("seconds", ctypes.c_double),
-                ("default_seconds", ctypes.c_double)]
+                ("default_seconds", ctypes.c_double), ("fp32_noprop_mask", ctypes.c_uint32)]
 
 
 class SidError(RuntimeError):
@@ -198,9 +198,10 @@ class Engine:
 
     def prove(self, lemma_id, generations=8, max_iterations=1, max_criticals=1 << 20, batch=0, precision=0,
               nargs=None, fetch=False, fp32_level_mask=0xFFFFFFFF, checkpoint=None, checkpoint_every=0, stop_after=0,
-              resume_from=None):
+              resume_from=None, fp32_noprop_mask=0):
         """A whole proof (sid_prove), or its continuation from a checkpoint file (resume_from, sid_prove_resume).
-        checkpoint/checkpoint_every/stop_after write checkpoints and stop early (result 'complete' False)."""
+        checkpoint/checkpoint_every/stop_after write checkpoints and stop early (result 'complete' False);
+        fp32_noprop_mask: float-pass levels without propagation (split-invariant form)."""
         opts = SidProveOpts()
         self.L.sid_prove_opts_default(ctypes.byref(opts))
         opts.generation_count = generations
@@ -209,6 +210,7 @@ class Engine:
         opts.batch_elements = batch
         opts.precision = precision
         opts.fp32_level_mask = fp32_level_mask
+        opts.fp32_noprop_mask = fp32_noprop_mask
         opts.checkpoint_path = checkpoint.encode() if checkpoint else None
         opts.checkpoint_every_steps = checkpoint_every
         opts.stop_after_steps = stop_after
@@ -251,7 +253,7 @@ class Engine:
         return dict(step_elements=t.step_elements, fp32_level_mask=t.fp32_level_mask,
                     escalation_threshold=t.escalation_threshold, levels=t.levels, candidates=t.candidates,
                     level_escalation=[t.level_escalation[k] for k in range(min(t.levels, MAX_LEVELS))],
-                    seconds=t.seconds, default_seconds=t.default_seconds)
+                    seconds=t.seconds, default_seconds=t.default_seconds, fp32_noprop_mask=t.fp32_noprop_mask)
 
     def batch_profile(self, enable):
         """Record CUDA events around the ordering and evaluation kernels of the following batch calls."""

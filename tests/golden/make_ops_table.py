@@ -67,7 +67,8 @@ def main():
         cnt = (ctypes.c_ulonglong * 6)()
         secs = ctypes.c_double()
         rc = L.sido_prove(sid.lemma_ir(name).encode(), ctypes.c_uint(8), ctypes.c_int(1), ctypes.c_float(0.25),
-                          ctypes.c_float(0.66), ctypes.c_int(8), ctypes.c_int(0), ctypes.c_uint(0xFFFFFFFF), cnt,
+                          ctypes.c_float(0.66), ctypes.c_int(8), ctypes.c_int(0), ctypes.c_uint(0xFFFFFFFF),
+                          ctypes.c_uint(0), cnt,
                           ctypes.byref(secs), None, ctypes.c_ulonglong(0), None)
         if rc != 0:
             raise RuntimeError("proof failed for " + name)

@@ -40,6 +40,40 @@ def test_precision_form_matches_oracle(engine, oracle, name):
     assert g["escalated"] < g["cuboids"]
 
 
+@pytest.mark.parametrize("name", ORACLE_FAST)
+def test_split_invariant_float_pass_matches_oracle(engine, oracle, name):
+    """Float pass without propagation on every level (k_prelude_f32 + k_filter_hoisted where the level has a
+    split-invariant form): counts and escalations equal the oracle's form without float propagation, and
+    the counts are the published ones."""
+    ir = sid.lemma_ir(name)
+    lid = engine.register(ir)
+    g = engine.prove(lid, precision=PRECISION_FP32, fp32_noprop_mask=0xFFFFFFFF)
+    o = oracle.prove(ir, fp32_first=True, fp32_noprop_mask=0xFFFFFFFF)
+    for k in ("cuboids", "leaves", "criticals", "escalated"):
+        assert g[k] == o[k], k
+    assert [g["cuboids"], g["leaves"]] == PUBLISHED[name]
+
+
+@pytest.mark.parametrize("name,gens", [("pos_neg1_sat", 7), ("run_prover_sat_f64", 11), ("pos_neg2_sat", 4)])
+def test_split_invariant_float_pass_criticals_match_oracle(engine, oracle, name, gens):
+    ir = sid.lemma_ir(name)
+    n = sid.ir_nargs(ir)
+    lid = engine.register(ir)
+    g = engine.prove(lid, generations=gens, nargs=n, fetch=True, precision=PRECISION_FP32, fp32_noprop_mask=0xFFFFFFFF)
+    o = oracle.prove(ir, generations=gens, max_criticals=1 << 20, fp32_first=True, fp32_noprop_mask=0xFFFFFFFF)
+    for k in ("cuboids", "leaves", "criticals", "escalated"):
+        assert g[k] == o[k], k
+    assert np.array_equal(bits(kat_expect.sort_boxes(g["boxes"])), bits(kat_expect.sort_boxes(o["boxes"])))
+
+
+def test_split_invariant_float_pass_acos_lemma(engine):
+    """The lemmas with acos keep their published counts with the split-invariant float pass."""
+    for name in ("more_subcontainers_2", "more_subcontainers_1"):
+        lid = engine.register(sid.lemma_ir(name))
+        r = engine.prove(lid, precision=PRECISION_FP32, fp32_noprop_mask=0xFFFFFFFF)
+        assert [r["cuboids"], r["leaves"]] == PUBLISHED[name] and r["criticals"] == 0
+
+
 def test_precision_form_acos_lemma_matches_oracle(engine, oracle):
     """The float pass bounds acos with acos_bound_f32 (sound, not correctly rounded); the oracle restates it, so
     the escalations of a lemma that uses acos (123 M cuboids; about a minute in the oracle) agree exactly."""

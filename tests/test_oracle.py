@@ -57,3 +57,14 @@ def test_oracle_root_box_inside_ct_bounds(oracle):
     box = oracle.root_box(ir, 3)
     assert box[0, 0] == 0.295 or abs(box[0, 0] - 0.295) < 1e-15
     assert np.all(box[:, 0] <= box[:, 1])
+
+
+@pytest.mark.parametrize("name", ["one_subcontainer", "two_subcontainer", "five_subcontainer", "seven_subcontainer"])
+def test_oracle_precision_form_without_float_propagation_keeps_published_counts(oracle, name):
+    """With the float pass testing rows on the unpropagated child box (every level), a float refutation implies
+    the double one, so counts are the published ones; escalations grow (fewer float refutations)."""
+    ir = sid.lemma_ir(name)
+    a = oracle.prove(ir, fp32_first=True)
+    b = oracle.prove(ir, fp32_first=True, fp32_noprop_mask=0xFFFFFFFF)
+    assert [b["cuboids"], b["leaves"]] == PUBLISHED[name] and b["criticals"] == 0
+    assert b["escalated"] >= a["escalated"]
