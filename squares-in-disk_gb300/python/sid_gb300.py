@@ -384,7 +384,7 @@ def synthetic_batch(root, n, seed=0x5EED0001):
 def main(argv=None):
     """Command line: prove a lemma once or more on GPU 0 and print the counts.
 
-      python sid_gb300.py prove <lemma> [--precision 0|1] [--repeat N] [--generations G]
+      python sid_gb300.py prove <lemma> [--precision 0|1|2] [--noprop MASK] [--repeat N] [--generations G]
     """
     import argparse
     ap = argparse.ArgumentParser(prog="sid_gb300.py")
@@ -394,11 +394,12 @@ def main(argv=None):
     p.add_argument("--precision", type=int, default=PRECISION_PLAIN)
     p.add_argument("--repeat", type=int, default=1)
     p.add_argument("--generations", type=int, default=8)
+    p.add_argument("--noprop", type=lambda v: int(v, 0), default=0, help="float-pass levels without propagation")
     args = ap.parse_args(argv)
     eng = Engine(0)
     lid = eng.register(lemma_ir(args.lemma))
     for _ in range(args.repeat):
-        r = eng.prove(lid, generations=args.generations, precision=args.precision)
+        r = eng.prove(lid, generations=args.generations, precision=args.precision, fp32_noprop_mask=args.noprop)
         print(args.lemma, "precision", args.precision, r, flush=True)
     eng.close()
     return 0
