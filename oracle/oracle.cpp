@@ -46,8 +46,8 @@ struct RoundDownScope {
 // Operation counting (the op-counting build, -DSIDO_COUNT_OPS, used to measure IEEE directed-rounding
 // operations per cuboid): additions/subtractions, multiplications, divisions, square roots, arc cosines.
 #ifdef SIDO_COUNT_OPS
-std::atomic<unsigned long long> g_ops[5];
-#define SIDO_COUNT(k) (g_ops[k].fetch_add(1, std::memory_order_relaxed))
+std::atomic<unsigned long long> g_ops[10];   // per kind, double then float
+#define SIDO_COUNT(k) (g_ops[(k) + (sizeof(T) == sizeof(float) ? 5 : 0)].fetch_add(1, std::memory_order_relaxed))
 #else
 #define SIDO_COUNT(k) ((void)0)
 #endif
@@ -874,9 +874,9 @@ template<class T> void eval_operands_t(const LemmaIR& L, const std::vector<int>&
 
 } // namespace
 
-void count_ops(unsigned long long out[5]) {
+void count_ops(unsigned long long out[10]) {
 #ifdef SIDO_COUNT_OPS
-    for(int k = 0; k < 5; ++k) out[k] = g_ops[k].exchange(0);
+    for(int k = 0; k < 10; ++k) out[k] = g_ops[k].exchange(0);
 #else
     throw std::runtime_error("oracle: built without SIDO_COUNT_OPS");
 #endif
@@ -895,7 +895,7 @@ void eval_operands(const std::string& ir, const double* lo, const double* hi, st
 }
 
 void eval_batch(const std::string& ir, const double* lo, const double* hi, std::uint64_t n,
-                double* out_lo, double* out_hi, std::int8_t* verdict, int threads) {
+                double* out_lo, double* out_hi, std::int8_t* verdict, int threads, bool float_rows_first) {
     LemmaIR L = sid::parse_lemma_ir(ir);
     if(L.numtype != "f64") throw std::invalid_argument("oracle eval_batch supports f64 lemmas");
     int nt = threads > 0 ? threads : int(std::max(1u, std::thread::hardware_concurrency()));
@@ -906,7 +906,9 @@ void eval_batch(const std::string& ir, const double* lo, const double* hi, std::
         try {
             RoundDownScope rd;
             Prover<double> P(L);
+            Prover<float> F(L);
             std::vector<Iv<double>> box(std::size_t(L.nargs));
+            std::vector<Iv<float>> fbox(std::size_t(L.nargs));
             const int last = L.nargs - 1;
             for(;;) {
                 std::uint64_t b = next.fetch_add(4096);
@@ -915,8 +917,19 @@ void eval_batch(const std::string& ir, const double* lo, const double* hi, std::
                 for(std::uint64_t i = b; i < e; ++i) {
                     for(int v = 0; v < L.nargs; ++v) box[std::size_t(v)] = {lo[std::uint64_t(v) * n + i], hi[std::uint64_t(v) * n + i], false};
                     std::int8_t vd = 0;
-                    if(P.propagate(last, box.data(), std::size_t(L.nargs), 4)) vd = 1;
-                    else if(!P.all_ok(box.data())) vd = 2;
+                    if(P.propagate(last, box.data(), std::size_t(L.nargs), 4)) {
+                        vd = 1;
+                    } else if(float_rows_first) {
+                        // the device's order: rows in float on the box rounded outward (round-down mode: a
+                        // cast rounds down, -cast(-x) up), in double only where float does not refute
+                        for(int v = 0; v < L.nargs; ++v) {
+                            const auto& b = box[std::size_t(v)];
+                            fbox[std::size_t(v)] = {static_cast<float>(b.lo), -static_cast<float>(-b.hi), false};
+                        }
+                        if(!F.all_ok(fbox.data()) || !P.all_ok(box.data())) vd = 2;
+                    } else if(!P.all_ok(box.data())) {
+                        vd = 2;
+                    }
                     verdict[i] = vd;
                     for(int v = 0; v < L.nargs; ++v) {
                         out_lo[std::uint64_t(v) * n + i] = box[std::size_t(v)].lo;

@@ -76,8 +76,10 @@ ProveResult prove(const std::string& ir, const ProveOptions& opt);
 
 /// Leaf evaluation of n boxes (structure of arrays lo[v*n+i]): propagate after a change of the last
 /// variable (it = nargs, rec = 4) and test all constraints. verdict: 0 survives, 1 empty, 2 violated.
+/// float_rows_first: test the constraints in float on the box rounded outward first, and in double only
+/// where float does not refute (the device's order; same results, used to count its operations).
 void eval_batch(const std::string& ir, const double* lo, const double* hi, std::uint64_t n,
-                double* out_lo, double* out_hi, std::int8_t* verdict, int threads);
+                double* out_lo, double* out_hi, std::int8_t* verdict, int threads, bool float_rows_first = false);
 
 /// Node ids of the expressions compared by the constraints' runtime comparisons (left, right per
 /// comparison; constraints in table order, predicate trees in pre-order).
@@ -90,7 +92,7 @@ void eval_operands(const std::string& ir, const double* lo, const double* hi, st
 
 /// The op-counting build (-DSIDO_COUNT_OPS): IEEE directed-rounding operations executed since the last
 /// call (additions/subtractions, multiplications, divisions, square roots, arc cosines), then reset.
-void count_ops(unsigned long long out[5]);
+void count_ops(unsigned long long out[10]);   // per kind (see make_ops_table.py), double then float
 
 /// Initial runtime box (2*nargs doubles).
 std::vector<double> root_box(const std::string& ir);

@@ -66,9 +66,10 @@ int sido_root_box(const char* ir, double* out) {
 }
 
 int sido_eval_batch(const char* ir, const double* lo, const double* hi, unsigned long long n, double* out_lo,
-                    double* out_hi, signed char* verdict, int threads) {
+                    double* out_hi, signed char* verdict, int threads, int float_rows_first) {
     try {
-        sido::eval_batch(ir, lo, hi, n, out_lo, out_hi, reinterpret_cast<std::int8_t*>(verdict), threads);
+        sido::eval_batch(ir, lo, hi, n, out_lo, out_hi, reinterpret_cast<std::int8_t*>(verdict), threads,
+                         float_rows_first != 0);
         return 0;
     } catch(const std::exception& e) {
         last_error = e.what();
@@ -100,7 +101,8 @@ int sido_eval_operands(const char* ir, const double* lo, const double* hi, unsig
     }
 }
 
-/* Op-counting build only: operations since the last call (add/sub, mul, div, sqrt, acos); 0 or -1. */
+/* Op-counting build only: operations since the last call (add/sub, mul, div, sqrt, acos), ten counts: in
+ * double, then in float; 0 or -1. */
 int sido_count_ops(unsigned long long* out) {
     try {
         sido::count_ops(out);

@@ -34,7 +34,7 @@ def lib():
         _lib.sido_root_box.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
         _lib.sido_eval_batch.restype = ctypes.c_int
         _lib.sido_eval_batch.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_ulonglong,
-                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         _lib.sido_last_error.restype = ctypes.c_char_p
         _lib.sido_acos_rounded.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
         _lib.sido_acos_rounded_f32.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_void_p]
@@ -83,8 +83,9 @@ def root_box(ir_text, nargs):
     return out.reshape(nargs, 2)
 
 
-def eval_batch(ir_text, lo, hi, threads=0):
-    """lo, hi: float64 arrays of shape (nargs, n). Returns (out_lo, out_hi, verdict)."""
+def eval_batch(ir_text, lo, hi, threads=0, float_rows_first=False):
+    """lo, hi: float64 arrays of shape (nargs, n). Returns (out_lo, out_hi, verdict). float_rows_first: the
+    device's order (constraints in float first, in double where float does not refute); same results."""
     lo = np.ascontiguousarray(lo, dtype=np.float64)
     hi = np.ascontiguousarray(hi, dtype=np.float64)
     n = lo.shape[1]
@@ -92,7 +93,7 @@ def eval_batch(ir_text, lo, hi, threads=0):
     out_hi = np.empty_like(hi)
     verdict = np.empty(n, dtype=np.int8)
     rc = lib().sido_eval_batch(ir_text.encode(), lo.ctypes.data, hi.ctypes.data, n, out_lo.ctypes.data,
-                               out_hi.ctypes.data, verdict.ctypes.data, threads)
+                               out_hi.ctypes.data, verdict.ctypes.data, threads, 1 if float_rows_first else 0)
     if rc != 0:
         raise RuntimeError("oracle: " + _err())
     return out_lo, out_hi, verdict

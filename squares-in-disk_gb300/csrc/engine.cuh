@@ -517,7 +517,8 @@ struct BatchArgs {
 };
 
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
-/// (it_limit = nargs, rec_limit = 4) and test all constraints. Threads follow `order` when given (the
+/// (it_limit = nargs, rec_limit = 4) and test all constraints (in float first for double lemmas, then in
+/// double for the cuboids float does not refute). Threads follow `order` when given (the
 /// host orders each tile of 2^18 cuboids by the Morton code of the cuboids' positions, so that a warp's
 /// cuboids take the same branches, sign cases and propagation orders, while the permuted accesses stay in
 /// an L2-sized window); results go to each cuboid's own position.
@@ -531,8 +532,19 @@ template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(c
     #pragma unroll
     for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
     std::int8_t vd = 0;
-    if(propagate<L, T>(N - 1, box, N, 4)) vd = 1;
-    else if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
+    if(propagate<L, T>(N - 1, box, N, 4)) {
+        vd = 1;
+    } else if constexpr(sizeof(T) == sizeof(double)) {
+        // the rows first in float on the propagated box rounded outward: every float interval contains the
+        // double interval of the same node, so a float refutation is the double one, and the double rows
+        // run only for the cuboids float cannot refute (the verdict is the same bit for bit)
+        Iv<float> fb[N];
+        #pragma unroll
+        for(int v = 0; v < N; ++v) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
+        if(!L::template rows_ok<float>(N - 1, N, fb) || !L::template rows_ok<T>(N - 1, N, box)) vd = 2;
+    } else {
+        if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
+    }
     a.verdict[i] = vd;
     #pragma unroll
     for(int v = 0; v < N; ++v) {

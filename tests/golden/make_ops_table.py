@@ -3,7 +3,9 @@
 multiplications, divisions, square roots, arc cosines) per cuboid, counted by the op-counting build of the
 CPU oracle (oracle/_build/liboracle_ops.so, -DSIDO_COUNT_OPS):
   * "batch": leaf evaluation (propagation after a change of the last variable, all constraints) of a
-    seeded sample of bench.py's synthetic batch, per lemma;
+    seeded sample of bench.py's synthetic batch, per lemma, in the device's order: double operations with
+    the constraints tested in float first and in double only where float does not refute them ("batch_f32":
+    the float operations of that order; "batch_plain": double operations of the all-double order);
   * "proof": whole plain proofs of the lemmas the oracle proves in seconds, per cuboid considered.
 bench.py turns the One Subcontainer batch figure into an FP64 operation rate for its roofline line.
 
@@ -33,15 +35,17 @@ def main():
     import sid_gb300 as sid
     oracle_py.build()
     L = ctypes.CDLL(os.path.join(REPO, "oracle", "_build", "liboracle_ops.so"))
-    counts = (ctypes.c_ulonglong * 5)()
+    counts = (ctypes.c_ulonglong * 10)()
 
-    def take():
+    def take(which="f64"):
         if L.sido_count_ops(counts) != 0:
             raise RuntimeError("op counting failed")
-        return [int(c) for c in counts]
+        c = [int(x) for x in counts]
+        return c[:5] if which == "f64" else c[5:]
 
     take()
-    out = {"sample": SAMPLE, "seed": SEED, "kinds": KINDS, "batch": {}, "proof": {}}
+    out = {"sample": SAMPLE, "seed": SEED, "kinds": KINDS, "batch": {}, "batch_f32": {}, "batch_plain": {},
+           "proof": {}}
     for name in sid.lemma_names():
         ir = sid.lemma_ir(name)
         nargs = sid.ir_nargs(ir)
@@ -53,13 +57,19 @@ def main():
         hi = np.ascontiguousarray(hi)
         olo, ohi = np.empty_like(lo), np.empty_like(hi)
         vd = np.empty(SAMPLE, dtype=np.int8)
-        rc = L.sido_eval_batch(ir.encode(), ctypes.c_void_p(lo.ctypes.data), ctypes.c_void_p(hi.ctypes.data),
-                               ctypes.c_ulonglong(SAMPLE), ctypes.c_void_p(olo.ctypes.data),
-                               ctypes.c_void_p(ohi.ctypes.data), ctypes.c_void_p(vd.ctypes.data), ctypes.c_int(8))
-        if rc != 0:
-            raise RuntimeError("batch evaluation failed for " + name)
-        c = take()
-        out["batch"][name] = dict(zip(KINDS, [x / SAMPLE for x in c]), total=sum(c) / SAMPLE)
+        for float_first, key in ((0, "batch_plain"), (1, "batch")):
+            rc = L.sido_eval_batch(ir.encode(), ctypes.c_void_p(lo.ctypes.data), ctypes.c_void_p(hi.ctypes.data),
+                                   ctypes.c_ulonglong(SAMPLE), ctypes.c_void_p(olo.ctypes.data),
+                                   ctypes.c_void_p(ohi.ctypes.data), ctypes.c_void_p(vd.ctypes.data), ctypes.c_int(8),
+                                   ctypes.c_int(float_first))
+            if rc != 0:
+                raise RuntimeError("batch evaluation failed for " + name)
+            c = [int(x) for x in counts] if L.sido_count_ops(counts) == 0 else None
+            if c is None:
+                raise RuntimeError("op counting failed")
+            out[key][name] = dict(zip(KINDS, [x / SAMPLE for x in c[:5]]), total=sum(c[:5]) / SAMPLE)
+            if float_first:
+                out["batch_f32"][name] = dict(zip(KINDS, [x / SAMPLE for x in c[5:]]), total=sum(c[5:]) / SAMPLE)
     for name in PROOF_LEMMAS:
         r = oracle_py.prove(sid.lemma_ir(name))   # the normal library: warm-up only
         take()

@@ -68,3 +68,18 @@ def test_oracle_precision_form_without_float_propagation_keeps_published_counts(
     b = oracle.prove(ir, fp32_first=True, fp32_noprop_mask=0xFFFFFFFF)
     assert [b["cuboids"], b["leaves"]] == PUBLISHED[name] and b["criticals"] == 0
     assert b["escalated"] >= a["escalated"]
+
+
+@pytest.mark.parametrize("name", [n for n in sid.lemma_names() if "numtype f64" in sid.lemma_ir(n)])
+def test_oracle_batch_float_rows_first_is_exact(oracle, name):
+    """Testing the constraints in float on the propagated box rounded outward first (the device's batch order)
+    changes no verdict and no box: a float refutation is a double refutation."""
+    ir = sid.lemma_ir(name)
+    n = sid.ir_nargs(ir)
+    lo, hi = sid.synthetic_batch(oracle.root_box(ir, n), 1 << 14, seed=0x5EED0009)
+    a = oracle.eval_batch(ir, lo, hi)
+    b = oracle.eval_batch(ir, lo, hi, float_rows_first=True)
+    assert np.array_equal(a[2], b[2])
+    assert np.array_equal(a[0].view(np.uint64), b[0].view(np.uint64))
+    assert np.array_equal(a[1].view(np.uint64), b[1].view(np.uint64))
+    assert len(np.unique(a[2])) >= 2
