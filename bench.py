@@ -48,9 +48,6 @@ NCU_FP64_PIPE_ACTIVE = 0.835
 # FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
 FP64_LANES_PER_CLOCK = 304
 OPS_TABLE = os.path.join(REPO, "tests", "golden", "ops_per_cuboid.json")
-# kernels of one sid_eval_batch_device call: ordering keys + histogram, two block scans, scan add, bucket
-# scatter, evaluation
-LAUNCHES_PER_EVAL = 6
 
 
 def measured_peaks():
@@ -400,7 +397,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
-    prof_calls, order_ms, eval_ms = eng.batch_profile_read()
+    prof_calls, order_ms, eval_ms, launches = eng.batch_profile_read(with_launches=True)
     eng.batch_profile(False)
     ms = max_over_ranks(dist, ms)
     if dist:
@@ -468,7 +465,7 @@ def run_ours(args):
                      "kernel": "k_eval_batch (one_subcontainer, Morton-ordered)",
                      "kernel_ms": kernel_s * 1000.0, "ordering_ms_per_step": order_ms / max(prof_calls, 1),
                      "note": "algorithmic bytes; the kernel is limited by the FP64 pipe, not HBM (see DESIGN.md)"},
-        "gpu_launches": args.steps * LAUNCHES_PER_EVAL,
+        "gpu_launches": launches,
         "clocks": clk,
         "proof": {"lemma": LEMMA, "cuboids": best["cuboids"], "leaves": best["leaves"],
                   "criticals": best["criticals"], "seconds": best["seconds"],

@@ -180,10 +180,25 @@ int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, co
  * sid_eval_batch_profile(engine, 1) makes every following sid_eval_batch* call record CUDA events on its
  * stream around its evaluation kernel and around its ordering kernel; sid_eval_batch_profile_read waits
  * for the recorded events, returns the
- * number of calls and the summed device milliseconds of the ordering work and of the evaluation kernel,
- * and clears the record (recording continues until sid_eval_batch_profile(engine, 0)). */
+ * number of calls, the summed device milliseconds of the ordering work and of the evaluation kernel, and the
+ * number of kernels those calls launched (ordering, evaluation, sample hand-over), and clears the record (recording continues until sid_eval_batch_profile(engine, 0)). */
 int sid_eval_batch_profile(sid_engine* engine, int enable);
-int sid_eval_batch_profile_read(sid_engine* engine, uint64_t* calls, double* order_ms, double* eval_ms);
+
+int sid_eval_batch_profile_read(sid_engine* engine, uint64_t* calls, double* order_ms, double* eval_ms,
+                                uint64_t* launches);
+
+/* Evaluation order of sid_eval_batch / sid_eval_batch_device for one lemma (no counterpart in the reference).
+ * Evaluating a batch in the Morton order of the cuboids' lower corners keeps the threads of a warp on the
+ * same branches of the double-precision constraints, which pays off when many cuboids need them, and costs
+ * a sort (about 0.6 ms per 2^24 cuboids on a GB300) otherwise; the order never changes a result.
+ * SID_BATCH_ORDER_AUTO (the default): each call whose predecessor's sample has arrived counts the cuboids
+ * whose constraints the float test could not decide, and later calls are ordered while that share exceeds
+ * 1 % (calls before the first sample arrives are ordered). mode < 0 keeps the mode; double_share (may be
+ * NULL) receives the last sampled share, -1 before any. */
+#define SID_BATCH_ORDER_AUTO 0
+#define SID_BATCH_ORDER_ON 1
+#define SID_BATCH_ORDER_OFF 2
+int sid_lemma_batch_order(sid_engine* engine, int lemma_id, int mode, double* double_share);
 
 /* Allocation-free leaf hulls. No counterpart in the reference: it is an addition of this library.
  *

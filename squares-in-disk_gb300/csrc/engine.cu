@@ -160,6 +160,23 @@ struct Lemma {
     bool tuned = false;                  // sid_lemma_autotune has chosen the precision-form configuration
     sid_tuning tuning{};
     std::vector<double> criticals;       // from the last sid_prove
+    // batch ordering of sid_eval_batch*: the mode, and the share of a sampled call's cuboids whose
+    // constraints the float test left to double (-1: no sample yet), read without blocking once the
+    // sampled call's copy of its counter has completed
+    int batch_order = SID_BATCH_ORDER_AUTO;
+    double batch_double_share = -1.0;
+    DevBuf<unsigned long long> batch_sample;
+    unsigned long long* batch_sample_host = nullptr;   // pinned
+    cudaEvent_t batch_sample_ev = nullptr;
+    bool batch_sample_pending = false;
+    std::uint64_t batch_sample_n = 0;
+    Lemma() = default;
+    Lemma(const Lemma&) = delete;
+    Lemma& operator=(const Lemma&) = delete;
+    ~Lemma() {
+        if(batch_sample_ev) cudaEventDestroy(batch_sample_ev);
+        if(batch_sample_host) cudaFreeHost(batch_sample_host);
+    }
 };
 
 using Clock = std::chrono::steady_clock;
@@ -954,6 +971,7 @@ struct sid_engine {
     DevBuf<std::uint32_t> batch_key, batch_order, batch_count, batch_totals;
     bool batch_profile = false;
     std::vector<cudaEvent_t> batch_events;   // four per profiled call: start, ordered, evaluated, scattered
+    std::uint64_t batch_launches = 0;        // kernels launched by profiled calls
 };
 
 namespace {
@@ -979,21 +997,56 @@ void profile_mark(sid_engine* eng, cudaStream_t s) {
 void profile_clear(sid_engine* eng) {
     for(cudaEvent_t ev : eng->batch_events) cudaEventDestroy(ev);
     eng->batch_events.clear();
+    eng->batch_launches = 0;
 }
 
 
-/// Evaluate a batch of n cuboids (SoA, device, variables `stride` apart; 0: n) in the order (tile of 2^18
-/// cuboids, Morton code of the lower corner); results go to the cuboids' own positions. Asynchronous on `s`.
+constexpr double kOrderShare = 0.01;   // AUTO orders batches when more cuboids than this need double constraints
+
+/// Hands a batch call's count of double-constraint cuboids to the host: a store into pinned host memory from
+/// the evaluation stream (no copy engine, so the sample never waits behind the large output copies), then
+/// the device counter is cleared for the next sampled call.
+__global__ void k_publish_sample(unsigned long long* dev, unsigned long long* host) {
+    if(blockIdx.x != 0 || threadIdx.x != 0) return;
+    *reinterpret_cast<volatile unsigned long long*>(host) = *dev;
+    *dev = 0;
+    __threadfence_system();
+}
+
+/// The share of cuboids that needed the double constraints in the lemma's last sampled batch call, if that
+/// call's counter has arrived (never blocks).
+void poll_batch_sample(Lemma* lem) {
+    if(!lem->batch_sample_pending) return;
+    const cudaError_t q = cudaEventQuery(lem->batch_sample_ev);
+    if(q == cudaErrorNotReady) {
+        if(cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();
+        return;
+    }
+    cuda_check(q, "batch sample");
+    lem->batch_double_share = double(*lem->batch_sample_host) / double(std::max<std::uint64_t>(lem->batch_sample_n, 1));
+    lem->batch_sample_pending = false;
+}
+
+/// Evaluate a batch of n cuboids (SoA, device, variables `stride` apart; 0: n); results go to the cuboids' own
+/// positions. Asynchronous on `s`. With ordering (the lemma's batch mode, see sid_lemma_batch_order) the
+/// cuboids are evaluated in the order (tile of 2^18 cuboids, Morton code of the lower corner), which keeps a
+/// warp's cuboids on the same branches of the double constraints; without it, in their own order, which
+/// saves the sort when the float test decides nearly every cuboid. Every call whose predecessor's sample has
+/// arrived counts the cuboids that needed the double constraints.
 void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const double* hi, std::uint64_t n, double* out_lo,
                         double* out_hi, std::int8_t* verdict, cudaStream_t s, std::uint64_t stride = 0) {
     if(stride == 0) stride = n;
     const int nargs = lem->ir.nargs;
     profile_mark(eng, s);
+    poll_batch_sample(lem);
+    const bool want_order = lem->batch_order == SID_BATCH_ORDER_ON ||
+                            (lem->batch_order == SID_BATCH_ORDER_AUTO &&
+                             (lem->batch_double_share < 0.0 || lem->batch_double_share > kOrderShare));
     const std::uint32_t* order = nullptr;
     const std::uint64_t tiles = (n + (std::uint64_t(1) << kTileLog) - 1) >> kTileLog;
     const std::uint64_t buckets = tiles << kTileKeyBits;
     const std::uint64_t blocks = (buckets + 4095) / 4096;
-    if(n >= 4096 && n <= 0xffffffffull && nargs <= 16 && blocks <= 4096) {
+    if(want_order && n >= 4096 && n <= 0xffffffffull && nargs <= 16 && blocks <= 4096) {
         const int bits = std::max(1, kTileKeyBits / std::max(nargs, 1));
         MortonQuant qp{};
         for(int v = 0; v < nargs; ++v) {
@@ -1015,10 +1068,30 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
         k_order_scatter<<<g, 256, 0, s>>>(eng->batch_key.p, n, eng->batch_count.p, eng->batch_order.p);
         cuda_check(cudaGetLastError(), "batch ordering");
         order = eng->batch_order.p;
+        if(eng->batch_profile) eng->batch_launches += 5;
     }
     profile_mark(eng, s);
-    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order, stride};
+    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order, stride, nullptr};
+    const bool sample = !lem->batch_sample_pending && !lem->k->is_f32 && n > 0;
+    if(sample) {
+        if(!lem->batch_sample_host) {   // once per lemma: pinned (device-visible) host word, cleared counter
+            cuda_check(cudaMallocHost(reinterpret_cast<void**>(&lem->batch_sample_host), sizeof(unsigned long long)),
+                       "batch sample");
+            cuda_check(cudaEventCreateWithFlags(&lem->batch_sample_ev, cudaEventDisableTiming), "batch sample");
+            lem->batch_sample.reserve(1);
+            cuda_check(cudaMemsetAsync(lem->batch_sample.p, 0, sizeof(unsigned long long), s), "batch sample");
+        }
+        a.double_rows = lem->batch_sample.p;
+    }
     cuda_check(lem->k->eval_batch(a, s), "eval batch");
+    if(eng->batch_profile) eng->batch_launches += n > 0 ? (sample ? 2 : 1) : 0;
+    if(sample) {
+        k_publish_sample<<<1, 1, 0, s>>>(lem->batch_sample.p, lem->batch_sample_host);
+        cuda_check(cudaGetLastError(), "batch sample");
+        cuda_check(cudaEventRecord(lem->batch_sample_ev, s), "batch sample");
+        lem->batch_sample_pending = true;
+        lem->batch_sample_n = n;
+    }
     profile_mark(eng, s);
     profile_mark(eng, s);
 }
@@ -1685,6 +1758,17 @@ int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid
     });
 }
 
+int sid_lemma_batch_order(sid_engine* engine, int lemma_id, int mode, double* double_share) {
+    return guarded([&] {
+        Lemma* l = get_lemma(engine, lemma_id);
+        if(mode > SID_BATCH_ORDER_OFF) fail(SID_ERR_INVALID, "unknown batch order mode %d", mode);
+        set_device(engine);
+        if(mode >= 0) l->batch_order = mode;
+        poll_batch_sample(l);
+        if(double_share) *double_share = l->batch_double_share;
+    });
+}
+
 int sid_eval_batch_profile(sid_engine* engine, int enable) {
     return guarded([&] {
         if(!engine) fail(SID_ERR_INVALID, "null engine");
@@ -1694,9 +1778,12 @@ int sid_eval_batch_profile(sid_engine* engine, int enable) {
     });
 }
 
-int sid_eval_batch_profile_read(sid_engine* engine, uint64_t* calls, double* order_ms, double* eval_ms) {
+int sid_eval_batch_profile_read(sid_engine* engine, uint64_t* calls, double* order_ms, double* eval_ms,
+                                uint64_t* launches) {
     return guarded([&] {
         if(!engine || !calls || !order_ms || !eval_ms) fail(SID_ERR_INVALID, "null argument");
+        if(launches) *launches = engine->batch_launches;
+        engine->batch_launches = 0;
         set_device(engine);
         *calls = 0;
         *order_ms = 0;

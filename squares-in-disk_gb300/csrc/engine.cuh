@@ -514,6 +514,7 @@ struct BatchArgs {
     std::uint64_t n;
     const std::uint32_t* order;   // thread t evaluates cuboid order[t] (nullptr: cuboid t)
     std::uint64_t stride;         // distance between variables in lo/hi/out_lo/out_hi (0: n)
+    unsigned long long* double_rows;   // if set: += cuboids whose constraints float could not refute
 };
 
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
@@ -526,12 +527,14 @@ template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(c
     constexpr int N = L::NARGS;
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if(t >= a.n) return;
+    const unsigned active = __activemask();
     const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
     Iv<T> box[N];
     const std::uint64_t st = a.stride ? a.stride : a.n;
     #pragma unroll
     for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
     std::int8_t vd = 0;
+    bool in_double = false;
     if(propagate<L, T>(N - 1, box, N, 4)) {
         vd = 1;
     } else if constexpr(sizeof(T) == sizeof(double)) {
@@ -541,7 +544,12 @@ template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(c
         Iv<float> fb[N];
         #pragma unroll
         for(int v = 0; v < N; ++v) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
-        if(!L::template rows_ok<float>(N - 1, N, fb) || !L::template rows_ok<T>(N - 1, N, box)) vd = 2;
+        if(!L::template rows_ok<float>(N - 1, N, fb)) {
+            vd = 2;
+        } else {
+            in_double = true;
+            if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
+        }
     } else {
         if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
     }
@@ -550,6 +558,10 @@ template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(c
     for(int v = 0; v < N; ++v) {
         a.out_lo[std::uint64_t(v) * st + i] = double(box[v].lo);
         a.out_hi[std::uint64_t(v) * st + i] = double(box[v].hi);
+    }
+    if(a.double_rows) {
+        const unsigned m = __ballot_sync(active, in_double);
+        if(m && int(lane_id()) == __ffs(active) - 1) atomicAdd(a.double_rows, (unsigned long long)__popc(m));
     }
 }
 

@@ -24,9 +24,10 @@ EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "si
             "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc", "sid_server_opts_default",
             "sid_server_create", "sid_server_destroy", "sid_submit", "sid_request_poll", "sid_request_wait",
             "sid_request_criticals", "sid_request_release", "sid_eval_batch_profile", "sid_eval_batch_profile_read",
-            "sid_lemma_autotune", "sid_prove_resume"]
+            "sid_lemma_autotune", "sid_prove_resume", "sid_lemma_batch_order"]
 
 PRECISION_PLAIN, PRECISION_FP32, PRECISION_TUNED = 0, 1, 2
+BATCH_ORDER_AUTO, BATCH_ORDER_ON, BATCH_ORDER_OFF = 0, 1, 2
 MAX_LEVELS = 16
 REQ_PENDING, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
@@ -126,9 +127,11 @@ def load(path=LIB_PATH):
                                         ctypes.POINTER(ctypes.c_uint64)]
     L.sid_request_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
     L.sid_eval_batch_profile.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.sid_lemma_batch_order.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     L.sid_lemma_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.POINTER(SidTuning)]
     L.sid_eval_batch_profile_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
-                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_uint64)]
     _lib = L
     return L
 
@@ -259,11 +262,20 @@ class Engine:
         """Record CUDA events around the ordering and evaluation kernels of the following batch calls."""
         _check(self.L.sid_eval_batch_profile(self.h, 1 if enable else 0))
 
-    def batch_profile_read(self):
-        """(calls, ordering ms, evaluation ms) summed over the recorded batch calls; clears the record."""
-        calls, a, b = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double()
-        _check(self.L.sid_eval_batch_profile_read(self.h, ctypes.byref(calls), ctypes.byref(a), ctypes.byref(b)))
-        return calls.value, a.value, b.value
+    def batch_order(self, lemma_id, mode=-1):
+        """Set the lemma's batch evaluation order (BATCH_ORDER_*; -1 keeps it); returns the last sampled share
+        of cuboids whose constraints needed double (-1 before any sample)."""
+        share = ctypes.c_double()
+        _check(self.L.sid_lemma_batch_order(self.h, lemma_id, mode, ctypes.byref(share)))
+        return share.value
+
+    def batch_profile_read(self, with_launches=False):
+        """(calls, ordering ms, evaluation ms[, kernels launched]) summed over the recorded batch calls; clears
+        the record."""
+        calls, a, b, k = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+        _check(self.L.sid_eval_batch_profile_read(self.h, ctypes.byref(calls), ctypes.byref(a), ctypes.byref(b),
+                                                  ctypes.byref(k)))
+        return (calls.value, a.value, b.value, k.value) if with_launches else (calls.value, a.value, b.value)
 
     def leaf_hull_noalloc(self, lemma_id, boxes_ptr, n, hulls_ptr, nonempty_ptr, leaves_ptr, stream=0):
         """Allocation-free leaf hulls on caller device buffers (see sid_leaf_hull_noalloc in sid.h)."""

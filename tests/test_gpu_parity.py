@@ -77,6 +77,28 @@ def test_host_batch_pipeline_equals_device_batch(engine, n):
     assert np.array_equal(bits(hhi), bits(o_hi.cpu().numpy()))
 
 
+@pytest.mark.parametrize("name", ["one_subcontainer", "seven_subcontainer", "more_subcontainers_2", "top_packing_1"])
+def test_batch_order_modes_give_identical_results(engine, name):
+    """Ordered, unordered and adaptive batch evaluation give the same verdicts and boxes bit for bit; after a
+    synchronous call the sampled share of cuboids that needed the double constraints is available."""
+    ir = sid.lemma_ir(name)
+    lid = engine.register(ir)
+    lo, hi = sid.synthetic_batch(engine.root_box(lid, sid.ir_nargs(ir)), 1 << 16, seed=0x5EED0007)
+    outs = []
+    for mode in (sid.BATCH_ORDER_ON, sid.BATCH_ORDER_OFF, sid.BATCH_ORDER_AUTO):
+        engine.batch_order(lid, mode)
+        outs.append(engine.eval_batch(lid, lo, hi))
+    for o in outs[1:]:
+        assert np.array_equal(o[2], outs[0][2])
+        assert np.array_equal(bits(o[0]), bits(outs[0][0])) and np.array_equal(bits(o[1]), bits(outs[0][1]))
+    share = engine.batch_order(lid)
+    assert 0.0 <= share <= 1.0
+    if name == "one_subcontainer":
+        assert share < 0.05      # the float test decides nearly every cuboid of this batch
+    with pytest.raises(sid.SidError):
+        engine.batch_order(lid, 7)
+
+
 @pytest.mark.parametrize("variant", ["f64", "f32"])
 def test_expected_criticals_kat(engine, variant):
     ir = sid.lemma_ir("expected_critical_" + variant)
