@@ -43,10 +43,12 @@ SEED = 0x5EED0001
 BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
 # DRAM bytes (read + write) of one k_eval_batch launch on this workload, from ncu
 # (profiles/k_eval_batch_one_subcontainer_2e24.md); traffic grows in proportion to the batch
-NCU_TRAFFIC_BYTES_2E24 = 1.461791e9 + 1.385948e9
-NCU_FP64_PIPE_ACTIVE = 0.835
+NCU_TRAFFIC_BYTES_2E24 = 0.809096e9 + 0.782796e9
+NCU_FP64_PIPE_ACTIVE = 0.470
 # FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
 FP64_LANES_PER_CLOCK = 304
+# FP32 lanes per clock of the whole GPU: 152 SMs x 128
+FP32_LANES_PER_CLOCK = 19456
 OPS_TABLE = os.path.join(REPO, "tests", "golden", "ops_per_cuboid.json")
 
 
@@ -462,9 +464,11 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC_BYTES_2E24 * n / float(1 << 24), "peak_kind": peak_kind,
                      "fp64_pipe_active_ncu": NCU_FP64_PIPE_ACTIVE,
-                     "kernel": "k_eval_batch (one_subcontainer, Morton-ordered)",
+                     "kernel": "k_eval_batch (one_subcontainer, float-first constraints, adaptive order)",
                      "kernel_ms": kernel_s * 1000.0, "ordering_ms_per_step": order_ms / max(prof_calls, 1),
-                     "note": "algorithmic bytes; the kernel is limited by the FP64 pipe, not HBM (see DESIGN.md)"},
+                     "note": "algorithmic bytes; DRAM traffic equals them (no re-reads); the kernel is bound by "
+                             "divergent instruction issue and its double propagation, not by HBM "
+                             "(profiles/k_eval_batch_one_subcontainer_2e24.md)"},
         "gpu_launches": launches,
         "clocks": clk,
         "proof": {"lemma": LEMMA, "cuboids": best["cuboids"], "leaves": best["leaves"],
@@ -472,17 +476,27 @@ def run_ours(args):
                   "cuboids_per_s": best["cuboids"] / best["seconds"]},
     }
     with open(OPS_TABLE) as f:
-        ops = json.load(f)["batch"][LEMMA]["total"]
+        table = json.load(f)
+    ops = table["batch"][LEMMA]["total"]
+    ops_f32 = table["batch_f32"][LEMMA]["total"]
     sm_mhz = (clk.get("sm_max_mhz") or 2070.0)
     peak_gops = FP64_LANES_PER_CLOCK * sm_mhz * 1e6 / 1e9
     achieved_gops = ops * n / kernel_s / 1e9
     line["roofline_fp64"] = {
         "ops_per_cuboid": ops, "achieved": achieved_gops, "peak": peak_gops, "unit": "G IEEE ops/s",
         "frac": achieved_gops / peak_gops, "pipe_active_ncu": NCU_FP64_PIPE_ACTIVE,
-        "note": "directed-rounding add/sub/mul/div/sqrt per cuboid from the op-counting oracle build "
-                "(tests/golden/ops_per_cuboid.json) over the evaluation kernel's time, against one FP64 "
-                "instruction per lane and clock; divisions, square roots, comparisons and selects cost more "
-                "FP64 instructions than they count here, hence the gap to the measured pipe activity"}
+        "note": "directed-rounding double add/sub/mul/div/sqrt per cuboid in the device's order (constraints in "
+                "float first) from the op-counting oracle build (tests/golden/ops_per_cuboid.json) over the "
+                "evaluation kernel's time, against one FP64 instruction per lane and clock; the double work "
+                "left is the propagation, whose comparisons, selects and conversions the count omits and "
+                "whose warps are divergent, hence the gap to the measured pipe activity"}
+    peak_f32 = FP32_LANES_PER_CLOCK * sm_mhz * 1e6 / 1e9
+    achieved_f32 = ops_f32 * n / kernel_s / 1e9
+    line["roofline_fp32"] = {
+        "ops_per_cuboid": ops_f32, "achieved": achieved_f32, "peak": peak_f32, "unit": "G IEEE ops/s",
+        "frac": achieved_f32 / peak_f32,
+        "note": "directed-rounding float operations per cuboid of the float constraint test, same table and "
+                "kernel time, against one FP32 instruction per lane and clock"}
     if lemma_set:
         line["lemma_set"] = lemma_set
     if serve:
