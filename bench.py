@@ -278,9 +278,8 @@ def serve_stream(eng, sid, precision, rates=SERVE_RATES, n_syn=SERVE_SYNTHETIC):
                 "subboxes": int(sum(len(b) for _, b in syn))}
             with open(PUBLISHED) as f:
                 pub = json.load(f)
-            if precision == PRECISION_PLAIN:
-                out["rate_%g" % rate]["whole_lemma_counts_match_published"] = all(
-                    [r["cuboids"], r["leaves"]] == pub[n] for (n, _), r in zip(whole, res_whole))
+            out["rate_%g" % rate]["whole_lemma_counts_match_published"] = all(
+                [r["cuboids"], r["leaves"]] == pub[n] for (n, _), r in zip(whole, res_whole))
     return out
 
 

@@ -517,13 +517,17 @@ struct BatchArgs {
     unsigned long long* double_rows;   // if set: += cuboids whose constraints float could not refute
 };
 
+#ifndef SID_BATCH_MIN_BLOCKS
+#define SID_BATCH_MIN_BLOCKS 8      // resident 128-thread blocks per SM the batch kernel is compiled for (64 registers)
+#endif
+
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
 /// (it_limit = nargs, rec_limit = 4) and test all constraints (in float first for double lemmas, then in
 /// double for the cuboids float does not refute). Threads follow `order` when given (the
 /// host orders each tile of 2^18 cuboids by the Morton code of the cuboids' positions, so that a warp's
 /// cuboids take the same branches, sign cases and propagation orders, while the permuted accesses stay in
 /// an L2-sized window); results go to each cuboid's own position.
-template<class L, class T> __global__ void __launch_bounds__(128) k_eval_batch(const BatchArgs a) {
+template<class L, class T> __global__ void __launch_bounds__(128, SID_BATCH_MIN_BLOCKS) k_eval_batch(const BatchArgs a) {
     constexpr int N = L::NARGS;
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if(t >= a.n) return;
