@@ -359,7 +359,11 @@ __device__ __forceinline__ void level_child(const LevelArgs& a, const std::uint6
     add_to_requests<RC_CUBOIDS, RC_LEAVES, -1>(active, a.req, tag, a.count_cuboids ? 1u : 0u, leaves, 0u);
 }
 
-template<class L, class T, int MODE> __global__ void __launch_bounds__(128) k_level(const LevelArgs a) {
+#ifndef SID_LEVEL_MIN_BLOCKS
+#define SID_LEVEL_MIN_BLOCKS 4      // resident 128-thread blocks per SM the plain-form level kernel is compiled for
+#endif
+
+template<class L, class T, int MODE> __global__ void __launch_bounds__(128, SID_LEVEL_MIN_BLOCKS) k_level(const LevelArgs a) {
     const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if(t >= total) return;
@@ -467,7 +471,11 @@ template<class L, class H> __global__ void __launch_bounds__(128, SID_FILTER_MIN
 
 /// Precision form, second pass: the escalated children, in double, with the plain form's outputs.
 /// Grid-stride over the list (its length is read on the device, so no host round trip is needed).
-template<class L, int MODE> __global__ void __launch_bounds__(128) k_level_esc(const LevelArgs a) {
+#ifndef SID_ESC_MIN_BLOCKS
+#define SID_ESC_MIN_BLOCKS 4        // resident 128-thread blocks per SM the double pass is compiled for (128 registers)
+#endif
+
+template<class L, int MODE> __global__ void __launch_bounds__(128, SID_ESC_MIN_BLOCKS) k_level_esc(const LevelArgs a) {
     const std::uint64_t n = *a.esc_count;
     const std::uint64_t stride = std::uint64_t(gridDim.x) * blockDim.x;
     for(std::uint64_t base = std::uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
