@@ -388,38 +388,68 @@ __device__ __forceinline__ void split_child_f32(float lb_lo, float ub_hi, float4
 #ifndef SID_FILTER_MIN_BLOCKS
 #define SID_FILTER_MIN_BLOCKS 8     // resident 128-thread blocks per SM the float pass is compiled for (64 registers)
 #endif
-/// End of a float-pass child: undecided children (ok) are appended to the escalation list (warp ballot),
-/// refuted ones count as leaves; every child counts as a cuboid of its request.
-__device__ __forceinline__ void filter_result(const LevelArgs& a, unsigned active, std::uint64_t item, std::uint64_t t,
-                                              bool ok) {
-    const unsigned m = __ballot_sync(active, ok);
-    const int leader = __ffs(active) - 1;
-    unsigned long long base = 0;
-    if(int(lane_id()) == leader && m) base = atomicAdd(a.esc_count, (unsigned long long)__popc(m));
-    base = __shfl_sync(active, base, leader);
-    if(ok) a.esc[base + __popc(m & lanes_below())] = std::uint32_t(t);
-    add_to_requests<RC_CUBOIDS, RC_LEAVES, RC_ESCALATED>(active, a.req, item_tag(a, item), 1u, ok ? 0u : 1u, ok ? 1u : 0u);
+/// End of a float-pass block (all 128 threads call it; `valid` is false past the chunk): undecided children
+/// (ok) are appended to the escalation list, refuted ones count as leaves, every child counts as a cuboid of
+/// its request. One escalation-list reservation per block, and, when the block's children all belong to one
+/// request (always for a whole-lemma proof), one update per counter per block: per-warp atomics on these
+/// few addresses would serialize in L2.
+__device__ __forceinline__ void filter_result_block(const LevelArgs& a, bool valid, std::uint32_t tag, std::uint64_t t,
+                                                    bool ok) {
+    __shared__ unsigned warp_esc[4];
+    __shared__ unsigned long long esc_base;
+    __shared__ std::uint32_t tag0;
+    const bool esc = valid && ok;
+    const unsigned m = __ballot_sync(0xffffffffu, esc);
+    const int w = int(threadIdx.x >> 5);
+    if(lane_id() == 0) warp_esc[w] = unsigned(__popc(m));
+    if(threadIdx.x == 0) tag0 = tag;
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        const unsigned total = warp_esc[0] + warp_esc[1] + warp_esc[2] + warp_esc[3];
+        esc_base = total ? atomicAdd(a.esc_count, (unsigned long long)total) : 0ull;
+    }
+    const bool one_request = __syncthreads_and(!valid || tag == tag0) != 0;   // also orders esc_base
+    unsigned off = 0;
+    for(int k = 0; k < w; ++k) off += warp_esc[k];
+    if(esc) a.esc[esc_base + off + __popc(m & lanes_below())] = std::uint32_t(t);
+    if(one_request) {
+        const int nvalid = __syncthreads_count(valid);
+        const int nesc = __syncthreads_count(esc);
+        if(threadIdx.x == 0 && nvalid > 0) {
+            ReqDev* r = a.req + tag0;
+            atomicAdd(&r->cnt[RC_CUBOIDS], (unsigned long long)nvalid);
+            if(nvalid > nesc) atomicAdd(&r->cnt[RC_LEAVES], (unsigned long long)(nvalid - nesc));
+            if(nesc > 0) atomicAdd(&r->cnt[RC_ESCALATED], (unsigned long long)nesc);
+        }
+    } else {
+        const unsigned active = __ballot_sync(0xffffffffu, valid);
+        if(valid) add_to_requests<RC_CUBOIDS, RC_LEAVES, RC_ESCALATED>(active, a.req, tag, 1u, ok ? 0u : 1u, ok ? 1u : 0u);
+    }
 }
 
 template<class L> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) k_filter_f32(const LevelArgs a) {
     constexpr int N = L::NARGS;
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if(t >= a.n_child) return;
-    const unsigned active = __activemask();
-    const std::uint64_t id = a.child_begin + t;
-    const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
-    const std::uint64_t j = id / std::uint64_t(a.nsub) - a.pitem_begin;
-    const int c = int(id % std::uint64_t(a.nsub));
-    Iv<float> box[N];
-    #pragma unroll
-    for(int v = 0; v < N; ++v) {
-        const float2 f = a.pbox[std::uint64_t(v) * a.pstride + j];
-        box[v] = {f.x, f.y, false};
-        if(v == a.var) split_child_f32(f.x, f.y, a.psplit[j], a.nsub, c, box[v].lo, box[v].hi);
+    const bool valid = t < a.n_child;
+    bool ok = false;
+    std::uint32_t tag = 0;
+    if(valid) {
+        const std::uint64_t id = a.child_begin + t;
+        const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
+        const std::uint64_t j = id / std::uint64_t(a.nsub) - a.pitem_begin;
+        const int c = int(id % std::uint64_t(a.nsub));
+        Iv<float> box[N];
+        #pragma unroll
+        for(int v = 0; v < N; ++v) {
+            const float2 f = a.pbox[std::uint64_t(v) * a.pstride + j];
+            box[v] = {f.x, f.y, false};
+            if(v == a.var) split_child_f32(f.x, f.y, a.psplit[j], a.nsub, c, box[v].lo, box[v].hi);
+        }
+        ok = a.fp32_noprop || !propagate<L, float>(a.var, box, a.it_limit, a.rec_limit);
+        if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<float>(a.row_begin, a.row_end, box);
+        tag = item_tag(a, item);
     }
-    bool ok = a.fp32_noprop || !propagate<L, float>(a.var, box, a.it_limit, a.rec_limit);
-    if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<float>(a.row_begin, a.row_end, box);
-    filter_result(a, active, item, t, ok);
+    filter_result_block(a, valid, tag, t, ok);
 }
 
 constexpr std::uint64_t kParentRefuted = 1ull << 63;
@@ -448,25 +478,29 @@ template<class L, class H> __global__ void __launch_bounds__(128) k_prelude_f32(
 template<class L, class H> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) k_filter_hoisted(const LevelArgs a) {
     constexpr int N = L::NARGS;
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if(t >= a.n_child) return;
-    const unsigned active = __activemask();
-    const std::uint64_t id = a.child_begin + t;
-    const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
-    const std::uint64_t j = id / std::uint64_t(a.nsub) - a.pitem_begin;
-    const int c = int(id % std::uint64_t(a.nsub));
-    const std::uint64_t bits = a.hbits[j];
-    bool ok = (bits & kParentRefuted) == 0;
-    if(ok) {
-        Iv<float> box[N];
-        #pragma unroll
-        for(int v = 0; v < N; ++v) {
-            const float2 f = a.pbox[std::uint64_t(v) * a.pstride + j];
-            box[v] = {f.x, f.y, false};
-            if(v == H::VAR) split_child_f32(f.x, f.y, a.psplit[j], a.nsub, c, box[v].lo, box[v].hi);
+    const bool valid = t < a.n_child;
+    bool ok = false;
+    std::uint32_t tag = 0;
+    if(valid) {
+        const std::uint64_t id = a.child_begin + t;
+        const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
+        const std::uint64_t j = id / std::uint64_t(a.nsub) - a.pitem_begin;
+        const int c = int(id % std::uint64_t(a.nsub));
+        const std::uint64_t bits = a.hbits[j];
+        ok = (bits & kParentRefuted) == 0;
+        if(ok) {
+            Iv<float> box[N];
+            #pragma unroll
+            for(int v = 0; v < N; ++v) {
+                const float2 f = a.pbox[std::uint64_t(v) * a.pstride + j];
+                box[v] = {f.x, f.y, false};
+                if(v == H::VAR) split_child_f32(f.x, f.y, a.psplit[j], a.nsub, c, box[v].lo, box[v].hi);
+            }
+            ok = H::child(box, a.hval, a.pstride, j, bits);
         }
-        ok = H::child(box, a.hval, a.pstride, j, bits);
+        tag = item_tag(a, item);
     }
-    filter_result(a, active, item, t, ok);
+    filter_result_block(a, valid, tag, t, ok);
 }
 
 /// Precision form, second pass: the escalated children, in double, with the plain form's outputs.
