@@ -268,12 +268,11 @@ __device__ __forceinline__ unsigned long long reserve_queue_slots(unsigned activ
     return slot;
 }
 
-/// One child c of item `item`: split, propagate, test rows, then emit / join / store. All lanes of
-/// `active` call this together (warp-aggregated atomics).
-template<class L, class T, int MODE>
-__device__ __forceinline__ void level_child(const LevelArgs& a, const std::uint64_t item, const int c, const unsigned active) {
+/// Child c of item `item` in T: split the item's variable (splitter.hpp:44-59), propagate, test the
+/// level's rows. Returns whether the child survives; `box` is its propagated box.
+template<class L, class T>
+__device__ __forceinline__ bool eval_child(const LevelArgs& a, const std::uint64_t item, const int c, Iv<T>* box) {
     constexpr int N = L::NARGS;
-    Iv<T> box[N];
     #pragma unroll
     for(int v = 0; v < N; ++v) {
         double2 b = a.in_box[std::uint64_t(v) * a.in_stride + item];
@@ -286,18 +285,97 @@ __device__ __forceinline__ void level_child(const LevelArgs& a, const std::uint6
     }
     bool ok = !propagate<L, T>(a.var, box, a.it_limit, a.rec_limit);
     if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<T>(a.row_begin, a.row_end, box);
+    return ok;
+}
 
-    const unsigned leaves = (MODE == MODE_HULL || MODE == MODE_CRIT) ? 1u : (ok ? 0u : 1u);
-    const std::uint32_t tag = item_tag(a, item);
+/// Output slots for the threads of a 128-thread block with `want` set, in thread order: one atomic per
+/// block on the shared counter (per-warp atomics on one address serialize in L2). All threads call it.
+__device__ __forceinline__ unsigned long long block_reserve(unsigned long long* counter, bool want) {
+    __shared__ unsigned warp_n[4];
+    __shared__ unsigned long long base_sh;
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    const int w = int(threadIdx.x >> 5);
+    if(lane_id() == 0) warp_n[w] = unsigned(__popc(m));
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        const unsigned total = warp_n[0] + warp_n[1] + warp_n[2] + warp_n[3];
+        base_sh = total ? atomicAdd(counter, (unsigned long long)total) : 0ull;
+    }
+    __syncthreads();
+    unsigned off = 0;
+    for(int k = 0; k < w; ++k) off += warp_n[k];
+    const unsigned long long slot = base_sh + off + __popc(m & lanes_below());
+    __syncthreads();   // warp_n and base_sh are free again for the next call
+    return slot;
+}
+
+/// Cuboid and leaf counts of a 128-thread block's children (all threads call it; the valid threads are a
+/// prefix of the block): one update per counter per block when they all belong to one request, else per warp.
+__device__ __forceinline__ void block_counts(const LevelArgs& a, bool valid, std::uint32_t tag, unsigned cub,
+                                             unsigned leaves) {
+    __shared__ std::uint32_t tag0;
+    if(threadIdx.x == 0) tag0 = tag;
+    __syncthreads();
+    if(__syncthreads_and(!valid || tag == tag0)) {
+        const int nc = __syncthreads_count(valid && cub != 0);
+        const int nl = __syncthreads_count(valid && leaves != 0);
+        if(threadIdx.x == 0) {
+            ReqDev* r = a.req + tag0;
+            if(nc) atomicAdd(&r->cnt[RC_CUBOIDS], (unsigned long long)nc);
+            if(nl) atomicAdd(&r->cnt[RC_LEAVES], (unsigned long long)nl);
+        }
+    } else {
+        const unsigned active = __ballot_sync(0xffffffffu, valid);
+        if(valid) add_to_requests<RC_CUBOIDS, RC_LEAVES, -1>(active, a.req, tag, cub, leaves, 0u);
+    }
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+    #pragma unroll
+    for(int o = 16; o > 0; o >>= 1) {
+        const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = u < v ? u : v;
+    }
+    return v;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+    #pragma unroll
+    for(int o = 16; o > 0; o >>= 1) {
+        const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = u > v ? u : v;
+    }
+    return v;
+}
+
+/// One child per thread (`valid` false past the input; the valid threads are a prefix): split, propagate,
+/// test rows, then emit / queue / join the element hull / store criticals, and count. BLOCK: all threads of
+/// the 128-thread block call this together, and output slots and counts are aggregated per block (the
+/// dense level kernel, where per-warp atomics on the shared counters serialize); otherwise all lanes of
+/// each warp call it and they are aggregated per warp, without block barriers (the escalated children).
+template<class L, class T, int MODE, bool BLOCK>
+__device__ __forceinline__ void level_child_block(const LevelArgs& a, const bool valid, const std::uint64_t item, const int c) {
+    constexpr int N = L::NARGS;
+    Iv<T> box[N];
+    bool ok = false;
+    std::uint32_t tag = 0;
+    if(valid) {
+        ok = eval_child<L, T>(a, item, c, box);
+        tag = item_tag(a, item);
+    }
+    const unsigned leaves = !valid ? 0u : ((MODE == MODE_HULL || MODE == MODE_CRIT) ? 1u : (ok ? 0u : 1u));
 
     if(MODE == MODE_EMIT) {
-        const unsigned m = __ballot_sync(active, ok);
-        const int leader = __ffs(active) - 1;
-        unsigned long long base = 0;
-        if(int(lane_id()) == leader && m) base = atomicAdd(a.out_count, (unsigned long long)__popc(m));
-        base = __shfl_sync(active, base, leader);
-        if(ok) {
-            const std::uint64_t slot = base + __popc(m & lanes_below());
+        const bool keep = valid && ok;
+        unsigned long long slot = 0;
+        if(BLOCK) {
+            slot = block_reserve(a.out_count, keep);
+        } else {
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            unsigned long long base = 0;
+            if(lane_id() == 0 && m) base = atomicAdd(a.out_count, (unsigned long long)__popc(m));
+            slot = __shfl_sync(0xffffffffu, base, 0) + __popc(m & lanes_below());
+        }
+        if(keep) {
             if(slot < a.out_cap) {
                 #pragma unroll
                 for(int v = 0; v < N; ++v) {
@@ -314,49 +392,76 @@ __device__ __forceinline__ void level_child(const LevelArgs& a, const std::uint6
                 atomicOr(a.overflow, 1u);
             }
         }
-    } else if(MODE == MODE_QUEUE) {
-        const unsigned long long slot = reserve_queue_slots(active, a.req, tag, ok);
-        if(ok) {
-            ReqDev* r = a.req + tag;
-            const unsigned long long cap = r->qcap;
-            if(slot < cap) {
-                #pragma unroll
-                for(int v = 0; v < N; ++v) r->qbox[std::uint64_t(v) * cap + slot] = make_double2(double(box[v].lo), double(box[v].hi));
-                const std::uint8_t d = a.in_depth ? a.in_depth[item] : a.depth_value;
-                r->qdepth[slot] = std::uint8_t(d + a.depth_add);
-            } else {
-                atomicAdd(&r->cnt[RC_OVERFLOW], 1ull);
+    } else {
+        const unsigned active = __ballot_sync(0xffffffffu, valid);
+        if(valid && MODE == MODE_QUEUE) {
+            const unsigned long long slot = reserve_queue_slots(active, a.req, tag, ok);
+            if(ok) {
+                ReqDev* r = a.req + tag;
+                const unsigned long long cap = r->qcap;
+                if(slot < cap) {
+                    #pragma unroll
+                    for(int v = 0; v < N; ++v) r->qbox[std::uint64_t(v) * cap + slot] = make_double2(double(box[v].lo), double(box[v].hi));
+                    const std::uint8_t d = a.in_depth ? a.in_depth[item] : a.depth_value;
+                    r->qdepth[slot] = std::uint8_t(d + a.depth_add);
+                } else {
+                    atomicAdd(&r->cnt[RC_OVERFLOW], 1ull);
+                }
             }
-        }
-    } else if(MODE == MODE_HULL) {
-        if(ok) {
+        } else if(valid && MODE == MODE_HULL) {
             const std::uint32_t e = item_elem(a, item);
             const std::uint64_t path = (a.in_path ? a.in_path[item] : 0ull) * std::uint64_t(a.nsub) + std::uint64_t(c);
-            #pragma unroll
-            for(int v = 0; v < N; ++v) {
-                const double lo = double(box[v].lo), hi = double(box[v].hi);
-                const std::uint64_t idx = std::uint64_t(e) * N + v;
-                atomicMin(&a.hull_lo[idx], order_key(lo));
-                atomicMax(&a.hull_hi[idx], order_key(hi));
-                if(lo == 0.0) atomicMin(&a.hull_zlo[idx], (path << 1) | (__double_as_longlong(lo) < 0 ? 1ull : 0ull));
-                if(hi == 0.0) atomicMin(&a.hull_zhi[idx], (path << 1) | (__double_as_longlong(hi) < 0 ? 1ull : 0ull));
-            }
-        }
-    } else if(MODE == MODE_CRIT) {
-        if(ok) {
-            ReqDev* r = a.req + tag;
-            const unsigned long long slot = atomicAdd(&r->cnt[RC_CRITICALS], 1ull);
-            if(slot < r->crit_cap) {
+            // a full warp of children of one element joins its hull with one atomic per bound: the minimum
+            // (maximum) over the warp equals the sequence of per-child atomicMin (atomicMax)
+            const bool one_elem = active == 0xffffffffu && __all_sync(0xffffffffu, e == __shfl_sync(0xffffffffu, e, 0));
+            const bool any_ok = __any_sync(active, ok);
+            if(any_ok) {
                 #pragma unroll
                 for(int v = 0; v < N; ++v) {
-                    r->crit[(slot * N + v) * 2] = double(box[v].lo);
-                    r->crit[(slot * N + v) * 2 + 1] = double(box[v].hi);
+                    const double lo = double(box[v].lo), hi = double(box[v].hi);
+                    const std::uint64_t idx = std::uint64_t(e) * N + v;
+                    unsigned long long klo = ok ? order_key(lo) : ~0ull, khi = ok ? order_key(hi) : 0ull;
+                    unsigned long long zlo = (ok && lo == 0.0) ? ((path << 1) | (__double_as_longlong(lo) < 0 ? 1ull : 0ull)) : ~0ull;
+                    unsigned long long zhi = (ok && hi == 0.0) ? ((path << 1) | (__double_as_longlong(hi) < 0 ? 1ull : 0ull)) : ~0ull;
+                    if(one_elem) {
+                        klo = warp_min_u64(klo);
+                        khi = warp_max_u64(khi);
+                        zlo = warp_min_u64(zlo);
+                        zhi = warp_min_u64(zhi);
+                        if(lane_id() == 0) {
+                            atomicMin(&a.hull_lo[idx], klo);
+                            atomicMax(&a.hull_hi[idx], khi);
+                            if(zlo != ~0ull) atomicMin(&a.hull_zlo[idx], zlo);
+                            if(zhi != ~0ull) atomicMin(&a.hull_zhi[idx], zhi);
+                        }
+                    } else if(ok) {
+                        atomicMin(&a.hull_lo[idx], klo);
+                        atomicMax(&a.hull_hi[idx], khi);
+                        if(zlo != ~0ull) atomicMin(&a.hull_zlo[idx], zlo);
+                        if(zhi != ~0ull) atomicMin(&a.hull_zhi[idx], zhi);
+                    }
+                }
+            }
+        } else if(valid && MODE == MODE_CRIT) {
+            if(ok) {
+                ReqDev* r = a.req + tag;
+                const unsigned long long slot = atomicAdd(&r->cnt[RC_CRITICALS], 1ull);
+                if(slot < r->crit_cap) {
+                    #pragma unroll
+                    for(int v = 0; v < N; ++v) {
+                        r->crit[(slot * N + v) * 2] = double(box[v].lo);
+                        r->crit[(slot * N + v) * 2 + 1] = double(box[v].hi);
+                    }
                 }
             }
         }
     }
-
-    add_to_requests<RC_CUBOIDS, RC_LEAVES, -1>(active, a.req, tag, a.count_cuboids ? 1u : 0u, leaves, 0u);
+    if(BLOCK) {
+        block_counts(a, valid, tag, (valid && a.count_cuboids) ? 1u : 0u, leaves);
+    } else {
+        const unsigned active = __ballot_sync(0xffffffffu, valid);
+        if(valid) add_to_requests<RC_CUBOIDS, RC_LEAVES, -1>(active, a.req, tag, a.count_cuboids ? 1u : 0u, leaves, 0u);
+    }
 }
 
 #ifndef SID_LEVEL_MIN_BLOCKS
@@ -366,9 +471,9 @@ __device__ __forceinline__ void level_child(const LevelArgs& a, const std::uint6
 template<class L, class T, int MODE> __global__ void __launch_bounds__(128, SID_LEVEL_MIN_BLOCKS) k_level(const LevelArgs a) {
     const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if(t >= total) return;
-    const unsigned active = __activemask();
-    level_child<L, T, MODE>(a, a.in_begin + t / std::uint64_t(a.nsub), int(t % std::uint64_t(a.nsub)), active);
+    const bool valid = t < total;
+    level_child_block<L, T, MODE, true>(a, valid, valid ? a.in_begin + t / std::uint64_t(a.nsub) : 0,
+                                        valid ? int(t % std::uint64_t(a.nsub)) : 0);
 }
 
 /// Float box of child c of a parent from its k_parent_f32 data: it contains the double child box of
@@ -512,13 +617,18 @@ template<class L, class H> __global__ void __launch_bounds__(128, SID_FILTER_MIN
 template<class L, int MODE> __global__ void __launch_bounds__(128, SID_ESC_MIN_BLOCKS) k_level_esc(const LevelArgs a) {
     const std::uint64_t n = *a.esc_count;
     const std::uint64_t stride = std::uint64_t(gridDim.x) * blockDim.x;
+    // warp-uniform rounds: every lane of a warp takes part in each of its warp's rounds
     for(std::uint64_t base = std::uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
         const std::uint64_t j = base + lane_id();
         const bool valid = j < n;
-        const unsigned active = __ballot_sync(0xffffffffu, valid);
-        if(!valid) continue;   // only in the warp's last round: base + stride >= n
-        const std::uint64_t id = a.child_begin + a.esc[j];
-        level_child<L, double, MODE>(a, a.in_begin + id / std::uint64_t(a.nsub), int(id % std::uint64_t(a.nsub)), active);
+        std::uint64_t item = 0;
+        int c = 0;
+        if(valid) {
+            const std::uint64_t id = a.child_begin + a.esc[j];
+            item = a.in_begin + id / std::uint64_t(a.nsub);
+            c = int(id % std::uint64_t(a.nsub));
+        }
+        level_child_block<L, double, MODE, false>(a, valid, item, c);
     }
 }
 
