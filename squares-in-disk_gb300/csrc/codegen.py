@@ -7,7 +7,8 @@ For every lemma IR file (written by the front end, include/ivarp/sid_fe/compile.
   * apply_bound<T>(k, box): evaluate bound function k on the box and apply it to its target
     variable (straight-line interval code, common subexpressions shared, if_then_else branches
     evaluated only when needed, like the reference's if_then_else evaluation);
-  * rows_ok<T>(r0, r1, box): do all constraints of rows [r0, r1) possibly hold (stops at the first
+  * rows_status<T>(r0, r1, box): 0 if a constraint of rows [r0, r1) cannot hold, 2 if all hold
+    definitely, else 1; rows_ok<T> is status != 0 (stops at the first
     violated constraint, like CPUProverCore::p_cuboid_violates_constraint_row);
   * the update lists as 64-bit masks, the targets and the compile-time variable bounds;
   * for double lemmas, per level that tests rows, the split-invariant form of the precision form's float
@@ -444,9 +445,12 @@ def generate(lemma):
         w("        }")
         w("    }")
     w("    template<class T> __device__ static int apply_bound(int k, Iv<T>* box);")
-    w("    template<class T> __device__ static bool rows_ok(int r0, int r1, const Iv<T>* box);")
+    w("    template<class T> __device__ static int rows_status(int r0, int r1, const Iv<T>* box);")
+    w("    template<class T> __device__ static bool rows_ok(int r0, int r1, const Iv<T>* box) {")
+    w("        return rows_status<T>(r0, r1, box) != 0;")
+    w("    }")
     for r in range(L.nargs):
-        w("    template<class T> __device__ static bool row_%d(const Iv<T>* box);" % r)
+        w("    template<class T> __device__ static int row_%d(const Iv<T>* box);" % r)
     w("};")
     w("")
     # bound functions
@@ -465,28 +469,31 @@ def generate(lemma):
     w("}")
     w("")
     for r in range(L.nargs):
-        w("template<class T> __device__ bool L::row_%d(const Iv<T>* box) {" % r)
+        w("template<class T> __device__ int L::row_%d(const Iv<T>* box) {" % r)
+        w("    bool all = true;")
         e = Emitter(L)
         scope = {}
         for ci in L.rows.get(r, []):
             p = e.pred(L.constraints[ci], scope)
-            e.emit("if(!%s.ub) return false;" % p)
+            e.emit("if(!%s.ub) return 0;" % p)
+            e.emit("all = all && %s.lb;" % p)
         out.extend(e.lines)
-        w("    return true;")
+        w("    return all ? 2 : 1;")
         w("}")
         w("")
-    w("template<class T> __device__ bool L::rows_ok(int r0, int r1, const Iv<T>* box) {")
+    w("template<class T> __device__ int L::rows_status(int r0, int r1, const Iv<T>* box) {")
+    w("    int status = 2;")
     w("    for(int r = r0; r < r1; ++r) {")
-    w("        bool ok = true;")
+    w("        int st = 2;")
     w("        switch(r) {")
     for r in range(L.nargs):
-        w("            case %d: ok = row_%d<T>(box); break;" % (r, r))
-        pass
+        w("            case %d: st = row_%d<T>(box); break;" % (r, r))
     w("            default: break;")
     w("        }")
-    w("        if(!ok) return false;")
+    w("        if(st == 0) return 0;")
+    w("        if(st == 1) status = 1;")
     w("    }")
-    w("    return true;")
+    w("    return status;")
     w("}")
     w("")
     hoisted = []
