@@ -93,11 +93,14 @@ typedef struct sid_prove_opts {
     uint32_t checkpoint_every_steps;    /* 0: only when stopping early */
     uint32_t stop_after_steps;          /* > 0: stop after this many steps (with a checkpoint) */
     uint32_t fp32_noprop_mask;          /* precision forms: float-pass levels that skip bound propagation and
-                                           test the rows on the child's float box (default none). Such a level
+                                           test the rows on the child's float box (default: all). Such a level
                                            cannot refute a child that double keeps: the float box then contains
-                                           the double box before and after its propagation. Levels with a
-                                           split-invariant form evaluate the subexpressions that do not depend
-                                           on the split variable once per parent. */
+                                           the double box before and after its propagation, so the counts are
+                                           the plain form's by construction. Levels with a split-invariant
+                                           form evaluate the subexpressions that do not depend on the split
+                                           variable once per parent. A level whose bit is clear propagates in
+                                           float first (fewer escalations; exact unless the float and double
+                                           propagations take different orders). */
 } sid_prove_opts;
 
 /* Fill `opts` with the defaults above. */
@@ -153,7 +156,8 @@ typedef struct sid_tuning {
     double level_escalation[SID_MAX_LEVELS];  /* measured escalation rate per level (-1: no children) */
     double seconds;                           /* proof time with the chosen configuration */
     double default_seconds;                   /* proof time with every level on the float pass, 65536 per step */
-    uint32_t fp32_noprop_mask;                /* float-pass levels without propagation (sid_prove_opts) */
+    uint32_t fp32_noprop_mask;                /* float-pass levels without propagation (sid_prove_opts; the
+                                                 default all, or propagation on some levels if faster) */
 } sid_tuning;
 
 int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid_tuning* out);

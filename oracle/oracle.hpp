@@ -61,8 +61,8 @@ struct ProveOptions {
                                      // evaluated in double, whose results are used
     std::uint32_t fp32_level_mask = ~0u;  // precision form: levels that use the float pass (bit d: dynamic
                                           // level d, bit D + j: static level j)
-    std::uint32_t fp32_noprop_mask = 0;   // precision form: float-pass levels that test the rows on the child's
-                                          // float box without bound propagation
+    std::uint32_t fp32_noprop_mask = ~0u; // precision form: float-pass levels that test the rows on the child's
+                                          // float box without bound propagation (the engine's default: all)
 };
 
 struct ProveResult {

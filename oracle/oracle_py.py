@@ -51,7 +51,7 @@ def _err():
 
 
 def prove(ir_text, generations=8, max_iterations=1, threads=0, max_criticals=0, nargs=None, fp32_first=False,
-          fp32_level_mask=0xFFFFFFFF, fp32_noprop_mask=0):
+          fp32_level_mask=0xFFFFFFFF, fp32_noprop_mask=0xFFFFFFFF):
     """Run the oracle proof; returns dict(cuboids, leaves, criticals, repeated, fp32_refuted, escalated, seconds,
     boxes). fp32_first selects the precision form (float first, double for what float cannot refute);
     fp32_noprop_mask its levels whose float pass skips bound propagation."""

@@ -699,6 +699,7 @@ struct Lane {
         if(!level_fp32) {
             LevelArgs a = a0;
             a.count_cuboids = true;
+            a.float_rows = fp32_first;   // precision form, level without the float pass: float-first rows
             cuda_check(lem->k->level(mode, a, st), "level kernel launch");
             return;
         }
@@ -1315,7 +1316,7 @@ struct sid_server {
             w->lane->configure(opts.step_elements > 0 ? std::uint64_t(opts.step_elements)
                                                       : (tuned ? std::uint64_t(lem->tuning.step_elements) : kDefaultStep),
                                opts.precision != SID_PRECISION_PLAIN, tuned ? lem->tuning.fp32_level_mask : ~0u,
-                               tuned ? lem->tuning.fp32_noprop_mask : 0u);
+                               tuned ? lem->tuning.fp32_noprop_mask : ~0u);
             Lane& lane = *w->lane;
             for(;;) {
                 std::vector<Request*> admit;
@@ -1431,7 +1432,7 @@ void sid_prove_opts_default(sid_prove_opts* o) {
     o->progress_first_ms = 8000;
     o->progress_every_ms = 2000;
     o->fp32_level_mask = ~0u;
-    o->fp32_noprop_mask = 0;
+    o->fp32_noprop_mask = ~0u;
 }
 
 const char* sid_last_error(void) { return g_last_error; }
@@ -1673,7 +1674,8 @@ int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid
         o.precision = SID_PRECISION_FP32_ESCALATE;
         o.max_criticals_kept = 0;
         double spent = 0;
-        std::uint32_t noprop = 0;
+        std::uint32_t noprop = ~0u;   // the default precision form: no float propagation
+        t.fp32_noprop_mask = ~0u;
         auto timed = [&](std::uint64_t step, std::uint32_t mask, sid_result& best) {
             for(int rep = 0; rep < 2; ++rep) {
                 sid_result r{};
@@ -1722,15 +1724,11 @@ int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid
                     t.escalation_threshold = cand.first;
                 }
             }
-            // float passes without propagation, in the split-invariant form: on every level that has one, or
-            // only on the innermost static level
-            std::uint32_t hoistable = 0;
-            for(int k = 0; k < std::min(levels, SID_MAX_LEVELS); ++k) {
-                if(l->k->hoist_values && l->k->hoist_values(k) >= 0) hoistable |= 1u << k;
-            }
+            // float passes with propagation: on every level, or on all but the innermost static level (whose
+            // split-invariant form is usually the fastest float pass)
             const std::uint32_t innermost = levels > 0 ? 1u << std::min(levels - 1, SID_MAX_LEVELS - 1) : 0u;
-            for(std::uint32_t cand : {hoistable & t.fp32_level_mask, hoistable & innermost & t.fp32_level_mask}) {
-                if(spent > max_seconds || cand == 0 || cand == t.fp32_noprop_mask) continue;
+            for(std::uint32_t cand : {0u, innermost}) {
+                if(spent > max_seconds || cand == t.fp32_noprop_mask) continue;
                 sid_result r{};
                 noprop = cand;
                 timed(kDefaultStep, t.fp32_level_mask, r);

@@ -210,6 +210,7 @@ struct LevelArgs {
     const float4* psplit;             // (RD(w), RU(lb), RU(w), 0) with w the double split width
     std::uint64_t pstride, pitem_begin;
     bool fp32_noprop;                 // float pass without bound propagation (rows only)
+    bool float_rows;                  // k_level in double: test the rows in float first (precision form)
     // split-invariant float pass (k_prelude_f32 / k_filter_hoisted): per parent j, stored subexpression
     // values hval[k*pstride + j] and their flags hbits[j] (kParentRefuted: no child can satisfy the rows)
     const float2* hval;
@@ -269,13 +270,14 @@ __device__ __forceinline__ unsigned long long reserve_queue_slots(unsigned activ
 }
 
 /// Child c of item `item` in T: split the item's variable (splitter.hpp:44-59), propagate, test the
-/// level's rows. Returns whether the child survives; `box` is its propagated box. FLOAT_ROWS (double
+/// level's rows. Returns whether the child survives; `box` is its propagated box. float_rows (double
 /// only): the rows are first tested in float on the propagated box rounded outward. Every float interval
 /// contains the double interval of the same node, so a float refutation is a double refutation and a
 /// float "every constraint holds definitely" makes every double constraint hold; only the remaining
 /// children test the rows in double. The result is the double result bit for bit.
-template<class L, class T, bool FLOAT_ROWS = false>
-__device__ __forceinline__ bool eval_child(const LevelArgs& a, const std::uint64_t item, const int c, Iv<T>* box) {
+template<class L, class T>
+__device__ __forceinline__ bool eval_child(const LevelArgs& a, const std::uint64_t item, const int c, Iv<T>* box,
+                                           const bool float_rows) {
     constexpr int N = L::NARGS;
     #pragma unroll
     for(int v = 0; v < N; ++v) {
@@ -289,12 +291,16 @@ __device__ __forceinline__ bool eval_child(const LevelArgs& a, const std::uint64
     }
     bool ok = !propagate<L, T>(a.var, box, a.it_limit, a.rec_limit);
     if(ok && a.row_end > a.row_begin) {
-        if constexpr(FLOAT_ROWS && sizeof(T) == sizeof(double)) {
-            Iv<float> fb[N];
-            #pragma unroll
-            for(int v = 0; v < N; ++v) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
-            const int st = L::template rows_status<float>(a.row_begin, a.row_end, fb);
-            ok = st == 2 || (st == 1 && L::template rows_ok<T>(a.row_begin, a.row_end, box));
+        if constexpr(sizeof(T) == sizeof(double)) {
+            if(float_rows) {
+                Iv<float> fb[N];
+                #pragma unroll
+                for(int v = 0; v < N; ++v) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
+                const int st = L::template rows_status<float>(a.row_begin, a.row_end, fb);
+                ok = st == 2 || (st == 1 && L::template rows_ok<T>(a.row_begin, a.row_end, box));
+            } else {
+                ok = L::template rows_ok<T>(a.row_begin, a.row_end, box);
+            }
         } else {
             ok = L::template rows_ok<T>(a.row_begin, a.row_end, box);
         }
@@ -366,14 +372,15 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 /// the 128-thread block call this together, and output slots and counts are aggregated per block (the
 /// dense level kernel, where per-warp atomics on the shared counters serialize); otherwise all lanes of
 /// each warp call it and they are aggregated per warp, without block barriers (the escalated children).
-template<class L, class T, int MODE, bool BLOCK, bool FLOAT_ROWS>
-__device__ __forceinline__ void level_child_block(const LevelArgs& a, const bool valid, const std::uint64_t item, const int c) {
+template<class L, class T, int MODE, bool BLOCK>
+__device__ __forceinline__ void level_child_block(const LevelArgs& a, const bool valid, const std::uint64_t item, const int c,
+                                                  const bool float_rows) {
     constexpr int N = L::NARGS;
     Iv<T> box[N];
     bool ok = false;
     std::uint32_t tag = 0;
     if(valid) {
-        ok = eval_child<L, T, FLOAT_ROWS>(a, item, c, box);
+        ok = eval_child<L, T>(a, item, c, box, float_rows);
         tag = item_tag(a, item);
     }
     const unsigned leaves = !valid ? 0u : ((MODE == MODE_HULL || MODE == MODE_CRIT) ? 1u : (ok ? 0u : 1u));
@@ -486,8 +493,8 @@ template<class L, class T, int MODE> __global__ void __launch_bounds__(128, SID_
     const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const bool valid = t < total;
-    level_child_block<L, T, MODE, true, false>(a, valid, valid ? a.in_begin + t / std::uint64_t(a.nsub) : 0,
-                                        valid ? int(t % std::uint64_t(a.nsub)) : 0);
+    level_child_block<L, T, MODE, true>(a, valid, valid ? a.in_begin + t / std::uint64_t(a.nsub) : 0,
+                                        valid ? int(t % std::uint64_t(a.nsub)) : 0, a.float_rows);
 }
 
 /// Float box of child c of a parent from its k_parent_f32 data: it contains the double child box of
@@ -642,7 +649,7 @@ template<class L, int MODE> __global__ void __launch_bounds__(128, SID_ESC_MIN_B
             item = a.in_begin + id / std::uint64_t(a.nsub);
             c = int(id % std::uint64_t(a.nsub));
         }
-        level_child_block<L, double, MODE, false, true>(a, valid, item, c);
+        level_child_block<L, double, MODE, false>(a, valid, item, c, true);
     }
 }
 

@@ -201,10 +201,10 @@ class Engine:
 
     def prove(self, lemma_id, generations=8, max_iterations=1, max_criticals=1 << 20, batch=0, precision=0,
               nargs=None, fetch=False, fp32_level_mask=0xFFFFFFFF, checkpoint=None, checkpoint_every=0, stop_after=0,
-              resume_from=None, fp32_noprop_mask=0):
+              resume_from=None, fp32_noprop_mask=None):
         """A whole proof (sid_prove), or its continuation from a checkpoint file (resume_from, sid_prove_resume).
         checkpoint/checkpoint_every/stop_after write checkpoints and stop early (result 'complete' False);
-        fp32_noprop_mask: float-pass levels without propagation (split-invariant form)."""
+        fp32_noprop_mask: float-pass levels without propagation (None: the engine default, all levels)."""
         opts = SidProveOpts()
         self.L.sid_prove_opts_default(ctypes.byref(opts))
         opts.generation_count = generations
@@ -213,7 +213,8 @@ class Engine:
         opts.batch_elements = batch
         opts.precision = precision
         opts.fp32_level_mask = fp32_level_mask
-        opts.fp32_noprop_mask = fp32_noprop_mask
+        if fp32_noprop_mask is not None:
+            opts.fp32_noprop_mask = fp32_noprop_mask
         opts.checkpoint_path = checkpoint.encode() if checkpoint else None
         opts.checkpoint_every_steps = checkpoint_every
         opts.stop_after_steps = stop_after
@@ -406,7 +407,8 @@ def main(argv=None):
     p.add_argument("--precision", type=int, default=PRECISION_PLAIN)
     p.add_argument("--repeat", type=int, default=1)
     p.add_argument("--generations", type=int, default=8)
-    p.add_argument("--noprop", type=lambda v: int(v, 0), default=0, help="float-pass levels without propagation")
+    p.add_argument("--noprop", type=lambda v: int(v, 0), default=None,
+                   help="float-pass levels without propagation (default: all)")
     args = ap.parse_args(argv)
     eng = Engine(0)
     lid = eng.register(lemma_ir(args.lemma))

@@ -1,6 +1,6 @@
-"""GPU tests of the precision form (SID_PRECISION_FP32_ESCALATE): every child cuboid is first propagated and
-tested in FP32 with outward rounding; only children FP32 cannot refute are evaluated in FP64, whose results
-are used.
+"""GPU tests of the precision form (SID_PRECISION_FP32_ESCALATE): every child cuboid is first tested in FP32
+with outward rounding (by default on its unpropagated float box, optionally after a float propagation); only
+children FP32 cannot refute are evaluated in FP64, whose results are used.
 
 The oracle restates the same form on the CPU (ProveOptions::fp32_first), so counts, the number of escalated
 children and the critical boxes must agree exactly. Every lemma must still be proved (no critical cuboid
@@ -74,6 +74,19 @@ def test_split_invariant_float_pass_acos_lemma(engine):
         assert [r["cuboids"], r["leaves"]] == PUBLISHED[name] and r["criticals"] == 0
 
 
+@pytest.mark.parametrize("name", ["one_subcontainer", "three_subcontainer", "five_subcontainer", "seven_subcontainer"])
+def test_propagating_float_pass_matches_oracle(engine, oracle, name):
+    """The float pass that propagates in float first on every level (fp32_noprop_mask 0): counts and escalations
+    equal the oracle's same form, and the counts are the published ones."""
+    ir = sid.lemma_ir(name)
+    lid = engine.register(ir)
+    g = engine.prove(lid, precision=PRECISION_FP32, fp32_noprop_mask=0)
+    o = oracle.prove(ir, fp32_first=True, fp32_noprop_mask=0)
+    for k in ("cuboids", "leaves", "criticals", "escalated"):
+        assert g[k] == o[k], k
+    assert [g["cuboids"], g["leaves"]] == PUBLISHED[name]
+
+
 def test_precision_form_acos_lemma_matches_oracle(engine, oracle):
     """The float pass bounds acos with acos_bound_f32 (sound, not correctly rounded); the oracle restates it, so
     the escalations of a lemma that uses acos (123 M cuboids; about a minute in the oracle) agree exactly."""
@@ -92,8 +105,8 @@ def test_precision_form_proves_every_lemma(engine, name):
     r = engine.prove(lid, precision=PRECISION_FP32)
     assert r["criticals"] == 0
     cuboids, leaves = PUBLISHED[name]
-    # float can refute a child that double does not only through a different propagation order; on
-    # these lemmas that never happens, so the counts are the published ones
+    # the default float pass tests unpropagated boxes, so a float refutation is a double one: the counts are
+    # the published ones by construction
     assert (r["cuboids"], r["leaves"]) == (cuboids, leaves)
 
 

@@ -61,11 +61,12 @@ def test_oracle_root_box_inside_ct_bounds(oracle):
 
 @pytest.mark.parametrize("name", ["one_subcontainer", "two_subcontainer", "five_subcontainer", "seven_subcontainer"])
 def test_oracle_precision_form_without_float_propagation_keeps_published_counts(oracle, name):
-    """With the float pass testing rows on the unpropagated child box (every level), a float refutation implies
-    the double one, so counts are the published ones; escalations grow (fewer float refutations)."""
+    """With the float pass testing rows on the unpropagated child box (every level, the default), a float
+    refutation implies the double one, so counts are the published ones; escalations grow against the form
+    that propagates in float first (fewer float refutations)."""
     ir = sid.lemma_ir(name)
-    a = oracle.prove(ir, fp32_first=True)
-    b = oracle.prove(ir, fp32_first=True, fp32_noprop_mask=0xFFFFFFFF)
+    a = oracle.prove(ir, fp32_first=True, fp32_noprop_mask=0)
+    b = oracle.prove(ir, fp32_first=True)
     assert [b["cuboids"], b["leaves"]] == PUBLISHED[name] and b["criticals"] == 0
     assert b["escalated"] >= a["escalated"]
 
