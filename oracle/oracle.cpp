@@ -485,17 +485,6 @@ template<class T> struct Prover {
         return true;
     }
     bool all_ok(const Iv<T>* box) { return rows_ok(L.nargs - 1, L.nargs, box); }
-    /// 0: a constraint of the last row cannot hold; 2: all hold definitely; 1: otherwise.
-    int last_row_status(const Iv<T>* box) {
-        ev.begin(box);
-        int status = 2;
-        for(int ci : L.rows[std::size_t(L.nargs - 1)]) {
-            const IB v = ev.evalp(L.constraints[std::size_t(ci)]);
-            if(!v.ub) return 0;
-            if(!v.lb) status = 1;
-        }
-        return status;
-    }
 };
 
 /// The provers one worker uses: the lemma's own number type, and for double lemmas in the precision form
@@ -937,8 +926,7 @@ void eval_batch(const std::string& ir, const double* lo, const double* hi, std::
                             const auto& b = box[std::size_t(v)];
                             fbox[std::size_t(v)] = {static_cast<float>(b.lo), -static_cast<float>(-b.hi), false};
                         }
-                        const int st = F.last_row_status(fbox.data());
-                        if(st == 0 || (st == 1 && !P.all_ok(box.data()))) vd = 2;
+                        if(!F.all_ok(fbox.data()) || !P.all_ok(box.data())) vd = 2;
                     } else if(!P.all_ok(box.data())) {
                         vd = 2;
                     }

@@ -77,8 +77,7 @@ ProveResult prove(const std::string& ir, const ProveOptions& opt);
 /// Leaf evaluation of n boxes (structure of arrays lo[v*n+i]): propagate after a change of the last
 /// variable (it = nargs, rec = 4) and test all constraints. verdict: 0 survives, 1 empty, 2 violated.
 /// float_rows_first: test the constraints in float on the box rounded outward first, and in double only
-/// where float neither refutes them nor finds them all definitely satisfied (the device's order; same
-/// results, used to count its operations).
+/// where float does not refute them (the device's order; same results, used to count its operations).
 void eval_batch(const std::string& ir, const double* lo, const double* hi, std::uint64_t n,
                 double* out_lo, double* out_hi, std::int8_t* verdict, int threads, bool float_rows_first = false);
 

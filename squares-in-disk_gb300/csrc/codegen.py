@@ -445,12 +445,15 @@ def generate(lemma):
         w("        }")
         w("    }")
     w("    template<class T> __device__ static int apply_bound(int k, Iv<T>* box);")
-    w("    template<class T> __device__ static int rows_status(int r0, int r1, const Iv<T>* box);")
+    w("    template<class T, bool ALL> __device__ static int rows_eval(int r0, int r1, const Iv<T>* box);")
+    w("    template<class T> __device__ static int rows_status(int r0, int r1, const Iv<T>* box) {")
+    w("        return rows_eval<T, true>(r0, r1, box);")
+    w("    }")
     w("    template<class T> __device__ static bool rows_ok(int r0, int r1, const Iv<T>* box) {")
-    w("        return rows_status<T>(r0, r1, box) != 0;")
+    w("        return rows_eval<T, false>(r0, r1, box) != 0;")
     w("    }")
     for r in range(L.nargs):
-        w("    template<class T> __device__ static int row_%d(const Iv<T>* box);" % r)
+        w("    template<class T, bool ALL> __device__ static int row_%d(const Iv<T>* box);" % r)
     w("};")
     w("")
     # bound functions
@@ -469,25 +472,26 @@ def generate(lemma):
     w("}")
     w("")
     for r in range(L.nargs):
-        w("template<class T> __device__ int L::row_%d(const Iv<T>* box) {" % r)
+        w("template<class T, bool ALL> __device__ int L::row_%d(const Iv<T>* box) {" % r)
         w("    bool all = true;")
         e = Emitter(L)
         scope = {}
         for ci in L.rows.get(r, []):
             p = e.pred(L.constraints[ci], scope)
             e.emit("if(!%s.ub) return 0;" % p)
-            e.emit("all = all && %s.lb;" % p)
+            e.emit("if constexpr(ALL) all = all && %s.lb;" % p)
         out.extend(e.lines)
-        w("    return all ? 2 : 1;")
+        w("    (void)all;")
+        w("    return (ALL && all) ? 2 : 1;")
         w("}")
         w("")
-    w("template<class T> __device__ int L::rows_status(int r0, int r1, const Iv<T>* box) {")
+    w("template<class T, bool ALL> __device__ int L::rows_eval(int r0, int r1, const Iv<T>* box) {")
     w("    int status = 2;")
     w("    for(int r = r0; r < r1; ++r) {")
     w("        int st = 2;")
     w("        switch(r) {")
     for r in range(L.nargs):
-        w("            case %d: st = row_%d<T>(box); break;" % (r, r))
+        w("            case %d: st = row_%d<T, ALL>(box); break;" % (r, r))
     w("            default: break;")
     w("        }")
     w("        if(st == 0) return 0;")

@@ -716,16 +716,14 @@ template<class L, class T> __global__ void __launch_bounds__(128, SID_BATCH_MIN_
         vd = 1;
     } else if constexpr(sizeof(T) == sizeof(double)) {
         // the rows first in float on the propagated box rounded outward: every float interval contains the
-        // double interval of the same node, so a float refutation is the double one and constraints that
-        // all hold definitely in float hold in double; the double rows run only for the other cuboids
-        // (the verdict is the same bit for bit)
+        // double interval of the same node, so a float refutation is the double one; the double rows run
+        // only for the cuboids float does not refute (the verdict is the same bit for bit)
         Iv<float> fb[N];
         #pragma unroll
         for(int v = 0; v < N; ++v) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
-        const int st = L::template rows_status<float>(N - 1, N, fb);
-        if(st == 0) {
+        if(!L::template rows_ok<float>(N - 1, N, fb)) {
             vd = 2;
-        } else if(st == 1) {   // neither refuted nor definitely satisfied in float
+        } else {   // not refuted in float (refutation alone: the all-definite test costs more than it saves here)
             in_double = true;
             if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
         }
