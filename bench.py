@@ -43,8 +43,8 @@ SEED = 0x5EED0001
 BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
 # DRAM bytes (read + write) of one k_eval_batch launch on this workload, from ncu
 # (profiles/k_eval_batch_one_subcontainer_2e24.md); traffic grows in proportion to the batch
-NCU_TRAFFIC_BYTES_2E24 = 0.809096e9 + 0.782796e9
-NCU_FP64_PIPE_ACTIVE = 0.470
+NCU_TRAFFIC_BYTES_2E24 = 0.816436e9 + 0.798974e9
+NCU_FP64_PIPE_ACTIVE = 0.518
 # FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
 FP64_LANES_PER_CLOCK = 304
 # FP32 lanes per clock of the whole GPU: 152 SMs x 128
