@@ -694,6 +694,12 @@ struct BatchArgs {
 #define SID_BATCH_MIN_BLOCKS 8      // resident 128-thread blocks per SM the batch kernel is compiled for (64 registers)
 #endif
 
+/// The double row test of the batch kernel, kept out of line: few cuboids reach it, and the kernel's hot
+/// code (double propagation, float rows) then fits the instruction cache better.
+template<class L, class T> __device__ __noinline__ bool rows_ok_outlined(int r0, int r1, const Iv<T>* box) {
+    return L::template rows_ok<T>(r0, r1, box);
+}
+
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
 /// (it_limit = nargs, rec_limit = 4) and test all constraints (in float first for double lemmas, then in
 /// double for the cuboids float does not refute). Threads follow `order` when given (the
@@ -725,7 +731,7 @@ template<class L, class T> __global__ void __launch_bounds__(128, SID_BATCH_MIN_
             vd = 2;
         } else {   // not refuted in float (refutation alone: the all-definite test costs more than it saves here)
             in_double = true;
-            if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
+            if(!rows_ok_outlined<L, T>(N - 1, N, box)) vd = 2;
         }
     } else {
         if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
