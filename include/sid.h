@@ -101,6 +101,11 @@ typedef struct sid_prove_opts {
                                            variable once per parent. A level whose bit is clear propagates in
                                            float first (fewer escalations; exact unless the float and double
                                            propagations take different orders). */
+    uint32_t part_index;                /* sharding (no counterpart in the reference): with part_count > 1, */
+    uint32_t part_count;                /* prove only the children i of the root partition's first split with
+                                           i % part_count == part_index. The parts' counts sum to the whole
+                                           proof's and their criticals together are the whole proof's, so
+                                           parts can run on separate GPUs or processes. 0 or 1: whole proof. */
 } sid_prove_opts;
 
 /* Fill `opts` with the defaults above. */

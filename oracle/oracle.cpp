@@ -592,13 +592,17 @@ template<class T> struct Driver {
         }
         const auto& s = dyn[d];
         int m = int(s.initial);
+        // sharding: the root's first split keeps only this part's children, and (as on the device) runs
+        // without the float pass
+        const bool sharded = d == 0 && opt.part_count > 1;
         for(int i = 0; i < m; ++i) {
+            if(sharded && std::uint32_t(i) % opt.part_count != opt.part_index) continue;
             ++c.cuboids;
             std::vector<Iv<T>> child = box;
             T lo, hi;
             split_point_pair(box[std::size_t(s.arg)].lo, box[std::size_t(s.arg)].hi, m, i, lo, hi);
             child[std::size_t(s.arg)] = {lo, hi, false};
-            if(refuted_in_fp32(S, c, box, s.arg, i, m, 2 * std::size_t(L.nargs), rec_limit,
+            if(!sharded && refuted_in_fp32(S, c, box, s.arg, i, m, 2 * std::size_t(L.nargs), rec_limit,
                                d + 1 == dyn.size() ? L.nargs - 1 : 0, d + 1 == dyn.size() ? L.nargs : 0, d)) {
                 ++c.leaves;
                 continue;

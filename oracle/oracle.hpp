@@ -63,6 +63,8 @@ struct ProveOptions {
                                           // level d, bit D + j: static level j)
     std::uint32_t fp32_noprop_mask = ~0u; // precision form: float-pass levels that test the rows on the child's
                                           // float box without bound propagation (the engine's default: all)
+    std::uint32_t part_index = 0;         // sharding: with part_count > 1 only the children i of the root's
+    std::uint32_t part_count = 0;         // first split with i % part_count == part_index
 };
 
 struct ProveResult {

@@ -19,16 +19,19 @@ const char* sido_last_error(void) { return last_error.c_str(); }
 /* counts_out: cuboids, leaves, criticals, repeated, fp32_refuted, escalated. crit_out may be NULL; it
  * receives up to crit_cap criticals (2*nargs doubles each); *crit_n receives the number of stored (lo,hi)
  * pairs. fp32_first selects the precision form, fp32_level_mask its levels that use the float pass,
- * fp32_noprop_mask those of them that skip bound propagation. */
+ * fp32_noprop_mask those of them that skip bound propagation; part_index/part_count shard the root
+ * partition's first split (part_count <= 1: whole proof). */
 int sido_prove(const char* ir, unsigned generations, int max_iterations, float vol, float single, int threads,
-               int fp32_first, unsigned fp32_level_mask, unsigned fp32_noprop_mask, unsigned long long* counts_out,
-               double* seconds,
+               int fp32_first, unsigned fp32_level_mask, unsigned fp32_noprop_mask, unsigned part_index,
+               unsigned part_count, unsigned long long* counts_out, double* seconds,
                double* crit_out, unsigned long long crit_cap, unsigned long long* crit_n) {
     try {
         sido::ProveOptions o;
         o.fp32_first = fp32_first != 0;
         o.fp32_level_mask = fp32_level_mask;
         o.fp32_noprop_mask = fp32_noprop_mask;
+        o.part_index = part_index;
+        o.part_count = part_count;
         o.generations = generations;
         o.max_iterations = max_iterations;
         o.iteration_volume = vol;

@@ -26,8 +26,8 @@ def lib():
         _lib = ctypes.CDLL(LIB)
         _lib.sido_prove.restype = ctypes.c_int
         _lib.sido_prove.argtypes = [ctypes.c_char_p, ctypes.c_uint, ctypes.c_int, ctypes.c_float, ctypes.c_float,
-                                    ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.c_uint,
-                                    ctypes.POINTER(ctypes.c_ulonglong),
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
+                                    ctypes.c_uint, ctypes.POINTER(ctypes.c_ulonglong),
                                     ctypes.POINTER(ctypes.c_double),
                                     ctypes.c_void_p, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)]
         _lib.sido_root_box.restype = ctypes.c_int
@@ -51,10 +51,11 @@ def _err():
 
 
 def prove(ir_text, generations=8, max_iterations=1, threads=0, max_criticals=0, nargs=None, fp32_first=False,
-          fp32_level_mask=0xFFFFFFFF, fp32_noprop_mask=0xFFFFFFFF):
+          fp32_level_mask=0xFFFFFFFF, fp32_noprop_mask=0xFFFFFFFF, part=None):
     """Run the oracle proof; returns dict(cuboids, leaves, criticals, repeated, fp32_refuted, escalated, seconds,
     boxes). fp32_first selects the precision form (float first, double for what float cannot refute);
-    fp32_noprop_mask its levels whose float pass skips bound propagation."""
+    fp32_noprop_mask its levels whose float pass skips bound propagation; part = (index, count) proves one
+    shard of the root partition's first split."""
     L = lib()
     counts = (ctypes.c_ulonglong * 6)()
     secs = ctypes.c_double()
@@ -65,7 +66,8 @@ def prove(ir_text, generations=8, max_iterations=1, threads=0, max_criticals=0, 
             nargs = int([l for l in ir_text.splitlines() if l.startswith("nargs ")][0].split()[1])
         buf = np.zeros(max_criticals * 2 * nargs, dtype=np.float64)
     rc = L.sido_prove(ir_text.encode(), generations, max_iterations, 0.25, 0.66, threads, 1 if fp32_first else 0,
-                      fp32_level_mask, fp32_noprop_mask, counts, ctypes.byref(secs),
+                      fp32_level_mask, fp32_noprop_mask, part[0] if part else 0, part[1] if part else 0, counts,
+                      ctypes.byref(secs),
                       buf.ctypes.data if buf is not None else None, max_criticals, ctypes.byref(n_pairs))
     if rc != 0:
         raise RuntimeError("oracle: " + _err())

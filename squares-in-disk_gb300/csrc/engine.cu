@@ -199,6 +199,7 @@ struct Request {
     Lemma* lem = nullptr;
     int slot = -1;
     bool full = true;                    // whole lemma (root partition) or sub-boxes
+    std::uint32_t part_index = 0, part_count = 0;   // whole lemma: only this part of the root partition
     const ProofState* resume = nullptr;  // continue from a checkpoint instead
     std::vector<double> boxes;           // sub-boxes, box-major (lo, hi) pairs
     std::uint64_t nboxes = 0;
@@ -443,6 +444,7 @@ struct Lane {
     bool fp32_first = false;
     std::uint32_t fp32_mask = ~0u;         // levels (dynamic d, static D + j) that use the float pass
     std::uint32_t noprop_mask = 0;         // float-pass levels without bound propagation (split-invariant form)
+    std::uint32_t root_part_index = 0, root_part_count = 0;   // the root partition being admitted (sharding)
     std::uint64_t fanout = 1, root_fanout = 1;
     int sm_count = 1;
     int max_slots = kDefaultSlots;
@@ -603,7 +605,12 @@ struct Lane {
         }
         cuda_check(cudaMemcpyAsync(req_dev.p + slot, &h, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
         cuda_check(cudaStreamSynchronize(st), "request slot");
-        if(r->full && !r->resume) run_dynamic(0, lem->root.p, 1, nullptr, nullptr, std::uint32_t(slot), 0, 1, true, 0);
+        if(r->full && !r->resume) {
+            root_part_index = r->part_index;
+            root_part_count = r->part_count;
+            run_dynamic(0, lem->root.p, 1, nullptr, nullptr, std::uint32_t(slot), 0, 1, true, 0);
+            root_part_index = root_part_count = 0;
+        }
         read_slots();
     }
 
@@ -694,7 +701,8 @@ struct Lane {
     void launch(int mode, const LevelArgs& a0, int level) {
         const std::uint64_t total = a0.n_in * std::uint64_t(a0.nsub);
         if(total == 0) return;
-        const bool level_fp32 = fp32_first && level < SID_MAX_LEVELS && ((fp32_mask >> level) & 1u);
+        // the root's first split of a sharded proof runs the dense kernel, which applies the part filter
+        const bool level_fp32 = fp32_first && level < SID_MAX_LEVELS && ((fp32_mask >> level) & 1u) && a0.part_count <= 1;
         if(level_fp32) level_children[std::size_t(level)] += total;
         if(!level_fp32) {
             LevelArgs a = a0;
@@ -794,6 +802,10 @@ struct Lane {
             a.nsub = nsub;
             a.it_limit = it_limit;
             a.rec_limit = rec_limit;
+            if(d == 0 && initial) {
+                a.part_index = root_part_index;
+                a.part_count = root_part_count;
+            }
             if(last) {
                 a.row_begin = n - 1;
                 a.row_end = n;
@@ -1172,10 +1184,15 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
                    mask_override ? *mask_override : (tuned ? lem->tuning.fp32_level_mask : o.fp32_level_mask),
                    noprop_override ? *noprop_override : (tuned ? lem->tuning.fp32_noprop_mask : o.fp32_noprop_mask));
 
+    if(o.part_count > 1 && o.part_index >= o.part_count) {
+        fail(SID_ERR_INVALID, "part_index %u outside part_count %u", o.part_index, o.part_count);
+    }
     Request r;
     r.lem = lem;
     r.lemma_id = lemma_id;
     r.full = true;
+    r.part_index = o.part_index;
+    r.part_count = o.part_count;
     r.generations = o.generation_count;
     r.crit_cap = o.max_criticals_kept;
     r.resume = resume;

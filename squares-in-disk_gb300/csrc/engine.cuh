@@ -211,6 +211,7 @@ struct LevelArgs {
     std::uint64_t pstride, pitem_begin;
     bool fp32_noprop;                 // float pass without bound propagation (rows only)
     bool float_rows;                  // k_level in double: test the rows in float first (precision form)
+    std::uint32_t part_index, part_count;   // part_count > 1: only children c with c % part_count == part_index
     // split-invariant float pass (k_prelude_f32 / k_filter_hoisted): per parent j, stored subexpression
     // values hval[k*pstride + j] and their flags hbits[j] (kParentRefuted: no child can satisfy the rows)
     const float2* hval;
@@ -329,12 +330,13 @@ __device__ __forceinline__ unsigned long long block_reserve(unsigned long long* 
     return slot;
 }
 
-/// Cuboid and leaf counts of a 128-thread block's children (all threads call it; the valid threads are a
-/// prefix of the block): one update per counter per block when they all belong to one request, else per warp.
+/// Cuboid and leaf counts of a 128-thread block's children (all threads call it): one update per counter per
+/// block when they all belong to one request, else per warp. Every valid thread writes its tag to tag0; when
+/// they differ, whichever value stays fails the uniformity test for some thread and the block falls back.
 __device__ __forceinline__ void block_counts(const LevelArgs& a, bool valid, std::uint32_t tag, unsigned cub,
                                              unsigned leaves) {
     __shared__ std::uint32_t tag0;
-    if(threadIdx.x == 0) tag0 = tag;
+    if(valid) tag0 = tag;
     __syncthreads();
     if(__syncthreads_and(!valid || tag == tag0)) {
         const int nc = __syncthreads_count(valid && cub != 0);
@@ -367,18 +369,21 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
     return v;
 }
 
-/// One child per thread (`valid` false past the input; the valid threads are a prefix): split, propagate,
-/// test rows, then emit / queue / join the element hull / store criticals, and count. BLOCK: all threads of
+/// One child per thread (`in_range` false past the input, then a prefix of the threads has children; with
+/// sharding only every part_count-th child is valid): split, propagate, test rows, then emit / queue / join
+/// the element hull / store criticals, and count. BLOCK: all threads of
 /// the 128-thread block call this together, and output slots and counts are aggregated per block (the
 /// dense level kernel, where per-warp atomics on the shared counters serialize); otherwise all lanes of
 /// each warp call it and they are aggregated per warp, without block barriers (the escalated children).
 template<class L, class T, int MODE, bool BLOCK>
-__device__ __forceinline__ void level_child_block(const LevelArgs& a, const bool valid, const std::uint64_t item, const int c,
+__device__ __forceinline__ void level_child_block(const LevelArgs& a, const bool in_range, const std::uint64_t item, const int c,
                                                   const bool float_rows) {
     constexpr int N = L::NARGS;
     Iv<T> box[N];
     bool ok = false;
     std::uint32_t tag = 0;
+    // a child outside the requested part (sharding of the root partition) does not exist for this proof
+    const bool valid = in_range && (a.part_count <= 1 || std::uint32_t(c) % a.part_count == a.part_index);
     if(valid) {
         ok = eval_child<L, T>(a, item, c, box, float_rows);
         tag = item_tag(a, item);
@@ -528,7 +533,7 @@ __device__ __forceinline__ void filter_result_block(const LevelArgs& a, bool val
     const unsigned m = __ballot_sync(0xffffffffu, esc);
     const int w = int(threadIdx.x >> 5);
     if(lane_id() == 0) warp_esc[w] = unsigned(__popc(m));
-    if(threadIdx.x == 0) tag0 = tag;
+    if(valid) tag0 = tag;   // any valid thread's tag; if they differ, the uniformity test below fails
     __syncthreads();
     if(threadIdx.x == 0) {
         const unsigned total = warp_esc[0] + warp_esc[1] + warp_esc[2] + warp_esc[3];

@@ -51,7 +51,8 @@ class SidProveOpts(ctypes.Structure):
                 ("progress_user", ctypes.c_void_p), ("progress_first_ms", ctypes.c_uint32),
                 ("progress_every_ms", ctypes.c_uint32), ("fp32_level_mask", ctypes.c_uint32),
                 ("checkpoint_path", ctypes.c_char_p), ("checkpoint_every_steps", ctypes.c_uint32),
-                ("stop_after_steps", ctypes.c_uint32), ("fp32_noprop_mask", ctypes.c_uint32)]
+                ("stop_after_steps", ctypes.c_uint32), ("fp32_noprop_mask", ctypes.c_uint32),
+                ("part_index", ctypes.c_uint32), ("part_count", ctypes.c_uint32)]
 
 
 class SidServerOpts(ctypes.Structure):
@@ -201,10 +202,11 @@ class Engine:
 
     def prove(self, lemma_id, generations=8, max_iterations=1, max_criticals=1 << 20, batch=0, precision=0,
               nargs=None, fetch=False, fp32_level_mask=0xFFFFFFFF, checkpoint=None, checkpoint_every=0, stop_after=0,
-              resume_from=None, fp32_noprop_mask=None):
+              resume_from=None, fp32_noprop_mask=None, part=None):
         """A whole proof (sid_prove), or its continuation from a checkpoint file (resume_from, sid_prove_resume).
         checkpoint/checkpoint_every/stop_after write checkpoints and stop early (result 'complete' False);
-        fp32_noprop_mask: float-pass levels without propagation (None: the engine default, all levels)."""
+        fp32_noprop_mask: float-pass levels without propagation (None: the engine default, all levels);
+        part = (index, count): prove one shard of the root partition (counts of all shards sum to the proof's)."""
         opts = SidProveOpts()
         self.L.sid_prove_opts_default(ctypes.byref(opts))
         opts.generation_count = generations
@@ -215,6 +217,8 @@ class Engine:
         opts.fp32_level_mask = fp32_level_mask
         if fp32_noprop_mask is not None:
             opts.fp32_noprop_mask = fp32_noprop_mask
+        if part is not None:
+            opts.part_index, opts.part_count = part
         opts.checkpoint_path = checkpoint.encode() if checkpoint else None
         opts.checkpoint_every_steps = checkpoint_every
         opts.stop_after_steps = stop_after

@@ -78,7 +78,7 @@ def main():
         secs = ctypes.c_double()
         rc = L.sido_prove(sid.lemma_ir(name).encode(), ctypes.c_uint(8), ctypes.c_int(1), ctypes.c_float(0.25),
                           ctypes.c_float(0.66), ctypes.c_int(8), ctypes.c_int(0), ctypes.c_uint(0xFFFFFFFF),
-                          ctypes.c_uint(0), cnt,
+                          ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_uint(0), cnt,
                           ctypes.byref(secs), None, ctypes.c_ulonglong(0), None)
         if rc != 0:
             raise RuntimeError("proof failed for " + name)

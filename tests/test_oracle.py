@@ -84,3 +84,12 @@ def test_oracle_batch_float_rows_first_is_exact(oracle, name):
     assert np.array_equal(a[0].view(np.uint64), b[0].view(np.uint64))
     assert np.array_equal(a[1].view(np.uint64), b[1].view(np.uint64))
     assert len(np.unique(a[2])) >= 2
+
+
+@pytest.mark.parametrize("name,parts", [("one_subcontainer", 3), ("three_subcontainer", 2), ("top_packing_2", 5)])
+def test_oracle_shards_sum_to_the_whole_proof(oracle, name, parts):
+    """Sharding the root partition's first split: the parts' counts add up to the published counts."""
+    ir = sid.lemma_ir(name)
+    res = [oracle.prove(ir, part=(i, parts)) for i in range(parts)]
+    assert [sum(r["cuboids"] for r in res), sum(r["leaves"] for r in res)] == PUBLISHED[name]
+    assert all(r["cuboids"] > 0 for r in res)
