@@ -6,6 +6,7 @@ module never falls back to anything else: if the library or a GPU is missing, ca
 import ctypes
 import glob
 import os
+import sys
 
 import numpy as np
 
@@ -398,10 +399,90 @@ def synthetic_batch(root, n, seed=0x5EED0001):
     return lo, hi
 
 
+def describe_ir(ir_text, root=None):
+    """A readable account of a compiled lemma, with the sections of the reference's print_prover_input
+    (prover_input/print_prover_input_impl.hpp:27-170): [Arguments] (split settings, compile-time bounds and,
+    if `root` (nargs x 2) is given, the initial runtime range), [Bounds] (the runtime bound table: target,
+    direction, bound function) and [Constraints] (the runtime constraint table, by row). Expressions are
+    printed in infix from the IR's nodes; constants as their double enclosure."""
+    import urllib.parse
+    sys.path.insert(0, os.path.join(PKG, "csrc"))
+    import codegen
+    import tempfile
+    with tempfile.NamedTemporaryFile("w", suffix=".sidir", delete=False) as f:
+        f.write(ir_text)
+        path = f.name
+    try:
+        L = codegen.Lemma(path)
+    finally:
+        os.unlink(path)
+    names = {}
+    for line in ir_text.splitlines():
+        t = line.split()
+        if t and t[0] == "arg":
+            names[int(t[1])] = urllib.parse.unquote(t[2])
+    infix = {"add": "+", "sub": "-", "mul": "*", "div": "/", "lt": "<", "le": "<=", "gt": ">", "ge": ">=",
+             "eq": "==", "ne": "!=", "orseq": "||", "andseq": "&&", "or": "|", "and": "&"}
+
+    def fx(v):
+        return "%.6f" % (v / 1e6) if abs(v) < 9223372036854775807 else ("inf" if v > 0 else "-inf")
+
+    def text(nid):
+        n = L.nodes[nid]
+        op = n.op
+        if op == "arg":
+            return names.get(n.aux, "x%d" % n.aux)
+        if op == "const":
+            lo, hi = float.fromhex(L.consts[n.aux][0]), float.fromhex(L.consts[n.aux][1])
+            return repr(lo) if lo == hi else "[%r, %r]" % (lo, hi)
+        if op == "bconst":
+            return "true" if n.aux else "false"
+        ch = [text(c) for c in n.ch]
+        if op in infix:
+            return "(" + (" %s " % infix[op]).join(ch) + ")"
+        if op == "neg":
+            return "-" + ch[0]
+        if op == "not":
+            return "!" + ch[0]
+        if op == "pow":
+            return "fixed_pow(%s, %d)" % (ch[0], n.aux)
+        if op == "ite":
+            return "if_then_else(%s, %s, %s)" % tuple(ch)
+        if op in ("min", "max"):
+            return ("minimum(" if op == "min" else "maximum(") + ", ".join(ch) + ")"
+        return "%s(%s)" % (op, ", ".join(ch))
+
+    out = ["[Arguments]"]
+    splits = {s[0]: s for s in L.splits}
+    for v in range(L.nargs):
+        sp = splits.get(v)
+        kind = ("Dynamic variable '%s', initial subs: %d, subs per subdivision: %d" % (names.get(v), sp[1], sp[2])
+                if sp and sp[3] else "Static variable '%s', subs per subdivision: %d" % (names.get(v), sp[2])
+                if sp else "Value '%s'" % names.get(v))
+        lo, hi = L.ct[v]
+        line = "    %d: %s, compile time bounds: [%s, %s]" % (v, kind, fx(lo), fx(hi))
+        if root is not None:
+            line += ", initial range: [%r, %r]" % (float(root[v][0]), float(root[v][1]))
+        out.append(line)
+    out.append("[Bounds]")
+    for k, (tgt, d, fn, defined) in enumerate(L.bounds):
+        rel = {1: "<=", 2: ">=", 3: "=="}[d]
+        out.append("    %d: '%s' %s %s%s" % (k, names.get(tgt), rel, text(fn), "" if defined else "  (maybe)"))
+    out.append("[Constraints]")
+    for r in range(L.nargs):
+        cs = L.rows.get(r, [])
+        if cs:
+            out.append("     %d arguments:" % (r + 1))
+            for ci in cs:
+                out.append("        " + text(L.constraints[ci]))
+    return "\n".join(out) + "\n"
+
+
 def main(argv=None):
     """Command line: prove a lemma once or more on GPU 0 and print the counts.
 
       python sid_gb300.py prove <lemma> [--precision 0|1|2] [--noprop MASK] [--repeat N] [--generations G]
+      python sid_gb300.py describe <lemma> [--root]
     """
     import argparse
     ap = argparse.ArgumentParser(prog="sid_gb300.py")
@@ -413,7 +494,19 @@ def main(argv=None):
     p.add_argument("--generations", type=int, default=8)
     p.add_argument("--noprop", type=lambda v: int(v, 0), default=None,
                    help="float-pass levels without propagation (default: all)")
+    q = sub.add_parser("describe", help="print a compiled lemma's arguments, bounds and constraints")
+    q.add_argument("lemma")
+    q.add_argument("--root", action="store_true", help="add the initial runtime range (needs the GPU engine)")
     args = ap.parse_args(argv)
+    if args.cmd == "describe":
+        ir = lemma_ir(args.lemma)
+        root = None
+        if args.root:
+            eng = Engine(0)
+            root = eng.root_box(eng.register(ir), ir_nargs(ir))
+            eng.close()
+        print(describe_ir(ir, root), end="")
+        return 0
     eng = Engine(0)
     lid = eng.register(lemma_ir(args.lemma))
     for _ in range(args.repeat):
