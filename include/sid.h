@@ -63,11 +63,11 @@ typedef void (*sid_progress_fn)(void* user, const sid_progress* progress);
 
 #define SID_PRECISION_PLAIN 0           /* the lemma's own number type, bit-exact with the reference */
 #define SID_PRECISION_FP32_ESCALATE 1   /* precision form for double lemmas: every child cuboid is first
-                                           propagated and tested in FP32 (outward rounded, sound); only
-                                           the children FP32 cannot refute are evaluated in FP64, whose
-                                           results are used. Counts equal the plain form's unless FP32
-                                           refutes a child FP64 would not (possible only through a
-                                           different propagation order); float lemmas run plain. */
+                                           tested in FP32 (outward rounded, sound); only the children FP32
+                                           cannot refute are evaluated in FP64, whose results are used. By
+                                           default the FP32 test skips propagation (fp32_noprop_mask), and
+                                           the counts are the plain form's by construction; float lemmas
+                                           run plain. */
 
 #define SID_PRECISION_FP32_TUNED 2      /* the precision form with the lemma's autotuned configuration
                                            (sid_lemma_autotune: step size, levels that use the float

@@ -43,6 +43,14 @@ class SidResult(ctypes.Structure):
 PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p)
 
 
+class SidProgress(ctypes.Structure):
+    _fields_ = [("queue_size", ctypes.c_uint64), ("cuboid_count", ctypes.c_uint64), ("leaf_count", ctypes.c_uint64),
+                ("critical_count", ctypes.c_uint64), ("queue_head", ctypes.POINTER(ctypes.c_double))]
+
+
+PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(SidProgress))
+
+
 class SidProveOpts(ctypes.Structure):
     _fields_ = [("generation_count", ctypes.c_uint32), ("max_iterations_per_node", ctypes.c_int32),
                 ("iteration_volume_criterion", ctypes.c_float),
@@ -203,11 +211,14 @@ class Engine:
 
     def prove(self, lemma_id, generations=8, max_iterations=1, max_criticals=1 << 20, batch=0, precision=0,
               nargs=None, fetch=False, fp32_level_mask=0xFFFFFFFF, checkpoint=None, checkpoint_every=0, stop_after=0,
-              resume_from=None, fp32_noprop_mask=None, part=None):
+              resume_from=None, fp32_noprop_mask=None, part=None, progress=None, progress_first_ms=None,
+              progress_every_ms=None):
         """A whole proof (sid_prove), or its continuation from a checkpoint file (resume_from, sid_prove_resume).
         checkpoint/checkpoint_every/stop_after write checkpoints and stop early (result 'complete' False);
         fp32_noprop_mask: float-pass levels without propagation (None: the engine default, all levels);
-        part = (index, count): prove one shard of the root partition (counts of all shards sum to the proof's)."""
+        part = (index, count): prove one shard of the root partition (counts of all shards sum to the proof's);
+        progress(dict): called between steps with queue_size, cuboids, leaves, criticals and queue_head (the
+        (lo, hi) pairs of one queued element, or None) after progress_first_ms, then every progress_every_ms."""
         opts = SidProveOpts()
         self.L.sid_prove_opts_default(ctypes.byref(opts))
         opts.generation_count = generations
@@ -220,6 +231,24 @@ class Engine:
             opts.fp32_noprop_mask = fp32_noprop_mask
         if part is not None:
             opts.part_index, opts.part_count = part
+        keep = None
+        if progress is not None:
+            n_vars = nargs
+
+            def _cb(_user, p):
+                q = p.contents
+                head = None
+                if q.queue_head and n_vars:
+                    head = np.ctypeslib.as_array(q.queue_head, shape=(2 * n_vars,)).reshape(n_vars, 2).copy()
+                progress(dict(queue_size=q.queue_size, cuboids=q.cuboid_count, leaves=q.leaf_count,
+                              criticals=q.critical_count, queue_head=head))
+
+            keep = PROGRESS_FN(_cb)
+            opts.progress = ctypes.cast(keep, ctypes.c_void_p)
+            if progress_first_ms is not None:
+                opts.progress_first_ms = progress_first_ms
+            if progress_every_ms is not None:
+                opts.progress_every_ms = progress_every_ms
         opts.checkpoint_path = checkpoint.encode() if checkpoint else None
         opts.checkpoint_every_steps = checkpoint_every
         opts.stop_after_steps = stop_after
