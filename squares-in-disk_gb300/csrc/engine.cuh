@@ -219,6 +219,24 @@ struct LevelArgs {
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+/// Parent offset q and child index c of child `id` of a level split nsub ways: a shift and a mask when nsub
+/// is a power of two (every fan-out of the shipped lemmas), else a 32-bit division (ids within one launch
+/// fit 32 bits), and a 64-bit division only beyond that.
+__device__ __forceinline__ void split_index(std::uint64_t id, int nsub, std::uint64_t& q, int& c) {
+    const unsigned n = unsigned(nsub);
+    if((n & (n - 1u)) == 0u) {
+        q = id >> (__ffs(int(n)) - 1);
+        c = int(id & std::uint64_t(n - 1u));
+    } else if(id <= 0xffffffffull) {
+        const unsigned i = unsigned(id), qq = i / n;
+        q = qq;
+        c = int(i - qq * n);
+    } else {
+        q = id / n;
+        c = int(id % n);
+    }
+}
 __device__ __forceinline__ unsigned lanes_below() { return (1u << lane_id()) - 1u; }
 
 __device__ __forceinline__ std::uint32_t item_elem(const LevelArgs& a, std::uint64_t item) {
@@ -498,8 +516,10 @@ template<class L, class T, int MODE> __global__ void __launch_bounds__(128, SID_
     const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
     const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const bool valid = t < total;
-    level_child_block<L, T, MODE, true>(a, valid, valid ? a.in_begin + t / std::uint64_t(a.nsub) : 0,
-                                        valid ? int(t % std::uint64_t(a.nsub)) : 0, a.float_rows);
+    std::uint64_t q = 0;
+    int c = 0;
+    if(valid) split_index(t, a.nsub, q, c);
+    level_child_block<L, T, MODE, true>(a, valid, a.in_begin + q, c, a.float_rows);
 }
 
 /// Float box of child c of a parent from its k_parent_f32 data: it contains the double child box of
@@ -566,9 +586,11 @@ template<class L> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) 
     std::uint32_t tag = 0;
     if(valid) {
         const std::uint64_t id = a.child_begin + t;
-        const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
-        const std::uint64_t j = id / std::uint64_t(a.nsub) - a.pitem_begin;
-        const int c = int(id % std::uint64_t(a.nsub));
+        std::uint64_t q;
+        int c;
+        split_index(id, a.nsub, q, c);
+        const std::uint64_t item = a.in_begin + q;
+        const std::uint64_t j = q - a.pitem_begin;
         Iv<float> box[N];
         #pragma unroll
         for(int v = 0; v < N; ++v) {
@@ -614,9 +636,11 @@ template<class L, class H> __global__ void __launch_bounds__(128, SID_FILTER_MIN
     std::uint32_t tag = 0;
     if(valid) {
         const std::uint64_t id = a.child_begin + t;
-        const std::uint64_t item = a.in_begin + id / std::uint64_t(a.nsub);
-        const std::uint64_t j = id / std::uint64_t(a.nsub) - a.pitem_begin;
-        const int c = int(id % std::uint64_t(a.nsub));
+        std::uint64_t q;
+        int c;
+        split_index(id, a.nsub, q, c);
+        const std::uint64_t item = a.in_begin + q;
+        const std::uint64_t j = q - a.pitem_begin;
         const std::uint64_t bits = a.hbits[j];
         ok = (bits & kParentRefuted) == 0;
         if(ok) {
@@ -651,8 +675,9 @@ template<class L, int MODE> __global__ void __launch_bounds__(128, SID_ESC_MIN_B
         int c = 0;
         if(valid) {
             const std::uint64_t id = a.child_begin + a.esc[j];
-            item = a.in_begin + id / std::uint64_t(a.nsub);
-            c = int(id % std::uint64_t(a.nsub));
+            std::uint64_t q;
+            split_index(id, a.nsub, q, c);
+            item = a.in_begin + q;
         }
         level_child_block<L, double, MODE, false>(a, valid, item, c, true);
     }
