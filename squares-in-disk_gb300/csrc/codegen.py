@@ -102,6 +102,17 @@ def fingerprint(text):
     return h
 
 
+CMP_OPS = {"lt", "le", "gt", "ge", "eq", "ne"}
+
+
+def cheap_constraint(L, nid):
+    """A constraint that only compares variables and constants (no arithmetic), or a constant one."""
+    n = L.nodes[nid]
+    if n.lb == n.ub:
+        return True
+    return n.op in CMP_OPS and all(L.nodes[c].op in ("arg", "const") for c in n.ch)
+
+
 def tri_nn(n):
     return 1 if n.lb >= 0 else (0 if n.ub <= 0 else -1)
 
@@ -454,6 +465,18 @@ def generate(lemma):
     w("    }")
     for r in range(L.nargs):
         w("    template<class T, bool ALL> __device__ static int row_%d(const Iv<T>* box);" % r)
+    rest_rows = sum(1 << r for r in range(L.nargs) if any(not cheap_constraint(L, L.constraints[ci])
+                                                          for ci in L.rows.get(r, [])))
+    w("    // rows_ok split in two: comparisons of variables and constants, and the constraints that compute")
+    w("    static constexpr std::uint64_t REST_ROWS = 0x%xull;   // rows with constraints that compute" % rest_rows)
+    w("    __device__ __forceinline__ static bool has_rest(int r0, int r1) {")
+    w("        return ((REST_ROWS >> r0) & ((1ull << (r1 - r0)) - 1)) != 0;")
+    w("    }")
+    w("    template<class T> __device__ static bool rows_cheap(int r0, int r1, const Iv<T>* box);")
+    w("    template<class T> __device__ static bool rows_rest(int r0, int r1, const Iv<T>* box);")
+    for r in range(L.nargs):
+        w("    template<class T> __device__ static bool rowc_%d(const Iv<T>* box);" % r)
+        w("    template<class T> __device__ static bool rowx_%d(const Iv<T>* box);" % r)
     w("};")
     w("")
     # bound functions
@@ -483,6 +506,33 @@ def generate(lemma):
         out.extend(e.lines)
         w("    (void)all;")
         w("    return (ALL && all) ? 2 : 1;")
+        w("}")
+        w("")
+    for r in range(L.nargs):
+        for cheap, fname in ((True, "rowc"), (False, "rowx")):
+            w("template<class T> __device__ bool L::%s_%d(const Iv<T>* box) {" % (fname, r))
+            e = Emitter(L)
+            scope = {}
+            for ci in L.rows.get(r, []):
+                if cheap_constraint(L, L.constraints[ci]) == cheap:
+                    p = e.pred(L.constraints[ci], scope)
+                    e.emit("if(!%s.ub) return false;" % p)
+            out.extend(e.lines)
+            w("    return true;")
+            w("}")
+            w("")
+    for fname, part in (("rows_cheap", "rowc"), ("rows_rest", "rowx")):
+        w("template<class T> __device__ bool L::%s(int r0, int r1, const Iv<T>* box) {" % fname)
+        w("    for(int r = r0; r < r1; ++r) {")
+        w("        bool ok = true;")
+        w("        switch(r) {")
+        for r in range(L.nargs):
+            w("            case %d: ok = %s_%d<T>(box); break;" % (r, part, r))
+        w("            default: break;")
+        w("        }")
+        w("        if(!ok) return false;")
+        w("    }")
+        w("    return true;")
         w("}")
         w("")
     w("template<class T, bool ALL> __device__ int L::rows_eval(int r0, int r1, const Iv<T>* box) {")
