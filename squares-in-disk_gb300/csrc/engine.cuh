@@ -72,6 +72,8 @@ template<> __device__ __forceinline__ Iv<float> cst<float>(double, double, float
     return {flo, fhi, und};
 }
 
+template<class L, class T> __device__ bool propagate_packed(int arg, Iv<T>* box, int it_limit, int rec_limit);
+
 /// Worklist bound propagation after a change of variable `arg` (both bounds), with the reference's
 /// FIFO order, de-duplication, per-bound recursion limit and "unstable" re-seeding between
 /// iterations (bound_propagation/iterated_recursive.hpp:59-131, dynamic_bound_application.hpp:104-123,
@@ -79,6 +81,7 @@ template<> __device__ __forceinline__ Iv<float> cst<float>(double, double, float
 template<class L, class T> __device__ bool propagate(int arg, Iv<T>* box, int it_limit, int rec_limit) {
     constexpr int NB = L::NBOUNDS;
     if(NB == 0) return false;
+    if constexpr(NB <= 16) return propagate_packed<L, T>(arg, box, it_limit, rec_limit);
     const std::uint64_t seed = L::upd_both(arg);
     if(!seed) return false;
     std::uint8_t ring[NB > 0 ? NB : 1];
@@ -137,6 +140,74 @@ template<class L, class T> __device__ bool propagate(int arg, Iv<T>* box, int it
         #pragma unroll
         for(int i = 0; i < NB; ++i) rec[i] = 0;
         unstable = 0;
+        nun = 0;
+    }
+    return false;
+}
+
+/// propagate for lemmas with at most 16 bounds, with the same order of bound applications, kept in
+/// registers: the FIFO and the unstable list are 4-bit bound ids packed into one 64-bit word each (head in
+/// the low nibble; a bound is queued at most once, so at most 16 entries), and the per-bound recursion
+/// counters are bytes of two 64-bit words (a counter grows only while below rec_limit <= 255, so it never
+/// carries into its neighbour). The byte arrays of the general form are indexed at run time and live in
+/// local memory.
+template<class L, class T> __device__ bool propagate_packed(int arg, Iv<T>* box, int it_limit, int rec_limit) {
+    static_assert(L::NBOUNDS <= 16, "packed worklist holds 16 bound ids");
+    const std::uint64_t seed = L::upd_both(arg);
+    if(!seed) return false;
+    std::uint64_t q = 0, ul = 0, rec0 = 0, rec1 = 0;
+    std::uint32_t present = 0, unstable = 0;
+    int qn = 0, nun = 0;
+    for(std::uint64_t m = seed; m; m &= m - 1) {
+        const int a = __ffsll((long long)m) - 1;
+        present |= 1u << a;
+        q |= std::uint64_t(a) << (4 * qn);
+        ++qn;
+    }
+    for(int it = 0; it < it_limit; ++it) {
+        while(qn > 0) {
+            const int k = int(q & 15u);
+            q >>= 4;
+            --qn;
+            present &= ~(1u << k);
+            const int r = L::template apply_bound<T>(k, box);
+            if(r == B_EMPTY) return true;
+            if(r == B_NONE) continue;
+            const int tgt = L::target(k);
+            std::uint64_t upd = r == B_LB ? L::upd_lb(tgt) : (r == B_UB ? L::upd_ub(tgt) : L::upd_both(tgt));
+            for(; upd; upd &= upd - 1) {
+                const int a = __ffsll((long long)upd) - 1;
+                const std::uint32_t bit = 1u << a;
+                const int sh = 8 * (a & 7);
+                const int ra = int(((a < 8 ? rec0 : rec1) >> sh) & 0xffu);
+                if(ra >= rec_limit) {
+                    if(!(present & bit) && !(unstable & bit)) {
+                        ul |= std::uint64_t(a) << (4 * nun);
+                        ++nun;
+                        unstable |= bit;
+                    }
+                } else if(!(present & bit)) {
+                    present |= bit;
+                    q |= std::uint64_t(a) << (4 * qn);
+                    ++qn;
+                    if(a < 8) rec0 += 1ull << sh;
+                    else rec1 += 1ull << sh;
+                }
+            }
+        }
+        if(nun == 0) break;
+        for(int j = 0; j < nun; ++j) {
+            const int a = int((ul >> (4 * j)) & 15u);
+            const std::uint32_t bit = 1u << a;
+            if(!(present & bit)) {
+                present |= bit;
+                q |= std::uint64_t(a) << (4 * qn);
+                ++qn;
+            }
+        }
+        rec0 = rec1 = 0;
+        unstable = 0;
+        ul = 0;
         nun = 0;
     }
     return false;
