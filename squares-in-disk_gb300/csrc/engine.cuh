@@ -802,7 +802,7 @@ template<class L, class T> __device__ __noinline__ bool rows_ok_outlined(int r0,
 }
 
 #ifndef SID_BATCH_TILES
-#define SID_BATCH_TILES 8           // 128-cuboid tiles per block of the batch kernel
+#define SID_BATCH_TILES 4           // 128-cuboid tiles per block of the batch kernel (1-16 measured, 4 fastest)
 #endif
 
 /// The second stage of the batch kernel for queue entry j: the constraints that compute, in float on the
