@@ -791,9 +791,17 @@ struct BatchArgs {
     unsigned long long* double_rows;   // if set: += cuboids whose constraints float could not refute
 };
 
-#ifndef SID_BATCH_MIN_BLOCKS
-#define SID_BATCH_MIN_BLOCKS 8      // resident 128-thread blocks per SM the batch kernel is compiled for (64 registers)
+/// Resident 128-thread blocks per SM the batch kernel is compiled for: 12 (42 registers) for lemmas with at
+/// most 3 variables, where the added warps hide more latency than the spills cost (One Subcontainer, 2^22
+/// cuboids: 0.225 -> 0.207 ms), 8 (64 registers) above (Four Subcontainer 0.174 ms at 8, 0.197 at 12).
+/// SID_BATCH_MIN_BLOCKS overrides it for tuning builds.
+template<class L> constexpr int batch_min_blocks() {
+#ifdef SID_BATCH_MIN_BLOCKS
+    return SID_BATCH_MIN_BLOCKS;
+#else
+    return L::NARGS <= 3 ? 12 : 8;
 #endif
+}
 
 /// The double row test of the batch kernel, kept out of line: few cuboids reach it, and the kernel's hot
 /// code (double propagation, float rows) then fits the instruction cache better.
@@ -844,7 +852,7 @@ template<class L, class T> __device__ __forceinline__ void batch_rest(const Batc
 /// batch), so stage 2 runs on full warps instead of on the few lanes of every warp that need it. Threads
 /// follow `order` when given (the host orders tiles of 2^18 cuboids by the Morton code of the cuboids'
 /// positions); results go to each cuboid's own position.
-template<class L, class T> __global__ void __launch_bounds__(128, SID_BATCH_MIN_BLOCKS) k_eval_batch(const BatchArgs a) {
+template<class L, class T> __global__ void __launch_bounds__(128, batch_min_blocks<L>()) k_eval_batch(const BatchArgs a) {
     constexpr int N = L::NARGS;
     constexpr int CAP = 256;
     __shared__ float2 qbox[N][CAP];
