@@ -813,49 +813,51 @@ template<class L, class T> __device__ __noinline__ bool rows_ok_outlined(int r0,
 #define SID_BATCH_TILES 4           // 128-cuboid tiles per block of the batch kernel (1-16 measured, 4 fastest)
 #endif
 
-/// The second stage of the batch kernel for queue entry j: the constraints that compute, in float on the
-/// entry's float box, then (double lemmas) all constraints in double on the propagated box the first stage
-/// wrote, for the cuboids float does not refute.
+/// The second stage of the batch kernel for queue entry j: the cuboid's propagated box, which the first
+/// stage wrote, rounded outward to float; the constraints that compute, in float; then (double lemmas) all
+/// constraints in double for the cuboids float does not refute.
 template<class L, class T> __device__ __forceinline__ void batch_rest(const BatchArgs& a, std::uint64_t first,
-                                                                      float2 (*qbox)[256],
                                                                       const std::uint32_t* qpos, int j,
                                                                       unsigned long long& n_double) {
     constexpr int N = L::NARGS;
     const std::uint64_t st = a.stride ? a.stride : a.n;
     const std::uint64_t t = first + qpos[j];
     const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
+    Iv<T> box[N];
     Iv<float> fb[N];
     #pragma unroll
-    for(int v = 0; v < N; ++v) fb[v] = {qbox[v][j].x, qbox[v][j].y, false};
+    for(int v = 0; v < N; ++v) {
+        box[v] = {T(a.out_lo[std::uint64_t(v) * st + i]), T(a.out_hi[std::uint64_t(v) * st + i]), false};
+        if constexpr(sizeof(T) == sizeof(double)) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
+        else fb[v] = {float(box[v].lo), float(box[v].hi), false};
+    }
     std::int8_t vd = 0;
     if(!L::template rows_rest<float>(N - 1, N, fb)) {
         vd = 2;
     } else if constexpr(sizeof(T) == sizeof(double)) {
         ++n_double;
-        Iv<T> box[N];
-        #pragma unroll
-        for(int v = 0; v < N; ++v) box[v] = {a.out_lo[std::uint64_t(v) * st + i], a.out_hi[std::uint64_t(v) * st + i], false};
         if(!rows_ok_outlined<L, T>(N - 1, N, box)) vd = 2;
     }
     a.verdict[i] = vd;
 }
 
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
-/// (it_limit = nargs, rec_limit = 4) and test all constraints, in float first for double lemmas (every
-/// float interval contains the double interval of the same node, so a float refutation is the double one)
-/// and in double for the cuboids float does not refute: the verdict is the double one bit for bit.
+/// (it_limit = nargs, rec_limit = 4) and test all constraints; the verdict is the double one bit for bit.
 /// Two stages per block of SID_BATCH_TILES tiles of 128 cuboids: (1) one thread per cuboid loads,
-/// propagates, writes the propagated box and tests the comparisons of variables and constants; the
-/// cuboids that pass and have constraints that compute go to a queue in shared memory with their float
-/// box; (2) whenever 128 entries are queued (and for the rest at the end) every thread takes one entry and
-/// tests the constraints that compute. Few cuboids reach stage 2 (~10 % of One Subcontainer's synthetic
-/// batch), so stage 2 runs on full warps instead of on the few lanes of every warp that need it. Threads
-/// follow `order` when given (the host orders tiles of 2^18 cuboids by the Morton code of the cuboids'
+/// propagates, writes the propagated box and tests the constraints that only compare variables and
+/// constants, in the lemma's own type (exact, and for double lemmas cheaper than rounding the box to
+/// float: GB300 issues double comparisons and conversions alike on its narrow FP64 pipe); the cuboids that
+/// pass and have constraints that compute go to a queue in shared memory; (2) whenever 128 entries are
+/// queued (and for the rest at the end) every thread takes one entry, rounds its box outward to float and
+/// tests the constraints that compute in float (every float interval contains the double interval of the
+/// same node, so a float refutation is the double one), and in double where float does not refute. Few
+/// cuboids reach stage 2 (~10 % of One Subcontainer's synthetic batch), so the conversions and the float
+/// constraints run on full warps instead of on the few lanes of every warp that need them. Threads follow
+/// `order` when given (the host orders tiles of 2^18 cuboids by the Morton code of the cuboids'
 /// positions); results go to each cuboid's own position.
 template<class L, class T> __global__ void __launch_bounds__(128, batch_min_blocks<L>()) k_eval_batch(const BatchArgs a) {
     constexpr int N = L::NARGS;
     constexpr int CAP = 256;
-    __shared__ float2 qbox[N][CAP];
     __shared__ std::uint32_t qpos[CAP];
     __shared__ int qn;
     const std::uint64_t st = a.stride ? a.stride : a.n;
@@ -869,7 +871,6 @@ template<class L, class T> __global__ void __launch_bounds__(128, batch_min_bloc
         if(base >= a.n) break;                                  // uniform over the block
         const std::uint64_t t = base + threadIdx.x;
         bool push = false;
-        Iv<float> fb[N];
         if(t < a.n) {
             const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
             Iv<T> box[N];
@@ -878,21 +879,11 @@ template<class L, class T> __global__ void __launch_bounds__(128, batch_min_bloc
             std::int8_t vd = 0;
             if(propagate<L, T>(N - 1, box, N, 4)) {
                 vd = 1;
-            } else {
-                #pragma unroll
-                for(int v = 0; v < N; ++v) {
-                    if constexpr(sizeof(T) == sizeof(double)) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
-                    else fb[v] = {float(box[v].lo), float(box[v].hi), false};
-                }
-                if(!L::template rows_cheap<float>(N - 1, N, fb)) {
-                    vd = 2;
-                } else if(rest) {
-                    push = true;
-                } else if constexpr(sizeof(T) == sizeof(double)) {
-                    ++n_double;
-                    if(!rows_ok_outlined<L, T>(N - 1, N, box)) vd = 2;
-                }
-            }
+            } else if(!L::template rows_cheap<T>(N - 1, N, box)) {
+                vd = 2;
+            } else if(rest) {
+                push = true;
+            }   // else every constraint of the row only compares, and the test above was the full one
             if(!push) a.verdict[i] = vd;
             #pragma unroll
             for(int v = 0; v < N; ++v) {
@@ -905,30 +896,22 @@ template<class L, class T> __global__ void __launch_bounds__(128, batch_min_bloc
             int at = 0;
             if(lane_id() == 0) at = atomicAdd(&qn, __popc(m));
             at = __shfl_sync(0xffffffffu, at, 0) + __popc(m & lanes_below());
-            if(push) {
-                #pragma unroll
-                for(int v = 0; v < N; ++v) qbox[v][at] = make_float2(fb[v].lo, fb[v].hi);
-                qpos[at] = std::uint32_t(t - first);
-            }
+            if(push) qpos[at] = std::uint32_t(t - first);
         }
         __syncthreads();                                        // the queue and the stage-1 outputs
         const int q = qn;
         __syncthreads();                                        // every warp has read qn before the next tile appends
         if(q >= 128) {
-            batch_rest<L, T>(a, first, qbox, qpos, int(threadIdx.x), n_double);
+            batch_rest<L, T>(a, first, qpos, int(threadIdx.x), n_double);
             __syncthreads();
             const int j = int(threadIdx.x) + 128;
-            if(j < q) {
-                #pragma unroll
-                for(int v = 0; v < N; ++v) qbox[v][threadIdx.x] = qbox[v][j];
-                qpos[threadIdx.x] = qpos[j];
-            }
+            if(j < q) qpos[threadIdx.x] = qpos[j];
             if(threadIdx.x == 0) qn = q - 128;
             __syncthreads();
         }
     }
     const int q = qn;
-    if(int(threadIdx.x) < q) batch_rest<L, T>(a, first, qbox, qpos, int(threadIdx.x), n_double);
+    if(int(threadIdx.x) < q) batch_rest<L, T>(a, first, qpos, int(threadIdx.x), n_double);
     if(a.double_rows) {
         const unsigned long long w = __reduce_add_sync(0xffffffffu, unsigned(n_double));
         if(lane_id() == 0 && w) atomicAdd(a.double_rows, w);
