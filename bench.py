@@ -43,8 +43,8 @@ SEED = 0x5EED0001
 BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
 # DRAM bytes (read + write) of one k_eval_batch launch on this workload, from ncu
 # (profiles/k_eval_batch_one_subcontainer_2e24.md); traffic grows in proportion to the batch
-NCU_TRAFFIC_BYTES_2E24 = 0.816436e9 + 0.798974e9
-NCU_FP64_PIPE_ACTIVE = 0.518
+NCU_TRAFFIC_BYTES_2E24 = 0.928059e9 + 1.072003e9
+NCU_FP64_PIPE_ACTIVE = 0.706
 # FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
 FP64_LANES_PER_CLOCK = 304
 # FP32 lanes per clock of the whole GPU: 152 SMs x 128
@@ -463,10 +463,12 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC_BYTES_2E24 * n / float(1 << 24), "peak_kind": peak_kind,
                      "fp64_pipe_active_ncu": NCU_FP64_PIPE_ACTIVE,
-                     "kernel": "k_eval_batch (one_subcontainer, float-first constraints, adaptive order)",
+                     "kernel": "k_eval_batch (one_subcontainer, two stages, adaptive order)",
                      "kernel_ms": kernel_s * 1000.0, "ordering_ms_per_step": order_ms / max(prof_calls, 1),
-                     "note": "algorithmic bytes; DRAM traffic equals them (no re-reads); the kernel is bound by "
-                             "divergent instruction issue and its double propagation, not by HBM "
+                     "note": "algorithmic bytes (97 per cuboid); DRAM traffic is 23 % above them (register "
+                             "spills at 12 resident blocks per SM, and stage 2 re-reads the boxes it queued); "
+                             "the kernel is bound by its FP64 pipe (71 % busy: the propagation's compares and "
+                             "the float conversions) and by latency, not by HBM "
                              "(profiles/k_eval_batch_one_subcontainer_2e24.md)"},
         "gpu_launches": launches,
         "clocks": clk,
@@ -484,8 +486,9 @@ def run_ours(args):
     line["roofline_fp64"] = {
         "ops_per_cuboid": ops, "achieved": achieved_gops, "peak": peak_gops, "unit": "G IEEE ops/s",
         "frac": achieved_gops / peak_gops, "pipe_active_ncu": NCU_FP64_PIPE_ACTIVE,
-        "note": "directed-rounding double add/sub/mul/div/sqrt per cuboid in the device's order (constraints in "
-                "float first) from the op-counting oracle build (tests/golden/ops_per_cuboid.json) over the "
+        "note": "directed-rounding double add/sub/mul/div/sqrt per cuboid with the constraints in float first "
+                "(the oracle's order; the device tests comparison-only constraints in double, which adds "
+                "compares, not arithmetic) from the op-counting oracle build (tests/golden/ops_per_cuboid.json) over the "
                 "evaluation kernel's time, against one FP64 instruction per lane and clock; the double work "
                 "left is the propagation, whose comparisons, selects and conversions the count omits and "
                 "whose warps are divergent, hence the gap to the measured pipe activity"}
