@@ -177,11 +177,12 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
                    double* out_lo, double* out_hi, int8_t* verdict);
 
 /* Same on device buffers, asynchronous on `stream` (a cudaStream_t; NULL for the legacy stream).
- * Within each tile of 2^18 consecutive cuboids the evaluation follows the Morton order of their lower
- * corners (computed on the device from the lemma's root box), which keeps a warp's cuboids on the same
- * code paths; every result is written to its cuboid's own position, so the output does not depend on the
- * order. The ordering scratch belongs to the engine: calls on one engine must not overlap on different
- * streams. */
+ * When the lemma's order is on (sid_lemma_batch_order; by default while more than 1 % of its cuboids need
+ * the double constraints) the evaluation follows, within each tile of 2^18 consecutive cuboids, the Morton
+ * order of their lower corners (computed on the device from the lemma's root box), which keeps a warp's
+ * cuboids on the same code paths; every result is written to its cuboid's own position, so the output does
+ * not depend on the order. The ordering scratch belongs to the engine: calls on one engine must not overlap
+ * on different streams. */
 int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
                           double* out_lo, double* out_hi, int8_t* verdict, void* stream);
 
