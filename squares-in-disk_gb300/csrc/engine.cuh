@@ -608,7 +608,7 @@ __device__ __forceinline__ void split_child_f32(float lb_lo, float ub_hi, float4
 /// sound as in double); every other child id goes to the escalation list, whose children are then
 /// evaluated in double by k_level_esc, with double results used throughout.
 #ifndef SID_FILTER_MIN_BLOCKS
-#define SID_FILTER_MIN_BLOCKS 8     // resident 128-thread blocks per SM the float pass is compiled for (64 registers)
+#define SID_FILTER_MIN_BLOCKS 12    // resident 128-thread blocks per SM the float passes are compiled for (40 registers)
 #endif
 /// End of a float-pass block (all 128 threads call it; `valid` is false past the chunk): undecided children
 /// (ok) are appended to the escalation list, refuted ones count as leaves, every child counts as a cuboid of
