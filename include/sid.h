@@ -191,7 +191,7 @@ int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, co
  * stream around its evaluation kernel and around its ordering kernel; sid_eval_batch_profile_read waits
  * for the recorded events, returns the
  * number of calls, the summed device milliseconds of the ordering work and of the evaluation kernel, and the
- * number of kernels those calls launched (ordering, evaluation, sample hand-over), and clears the record (recording continues until sid_eval_batch_profile(engine, 0)). */
+ * number of kernels those calls launched (ordering, evaluation, deferred evaluation, sample hand-over), and clears the record (recording continues until sid_eval_batch_profile(engine, 0)). */
 int sid_eval_batch_profile(sid_engine* engine, int enable);
 
 int sid_eval_batch_profile_read(sid_engine* engine, uint64_t* calls, double* order_ms, double* eval_ms,

@@ -113,6 +113,29 @@ def cheap_constraint(L, nid):
     return n.op in CMP_OPS and all(L.nodes[c].op in ("arg", "const") for c in n.ch)
 
 
+SLOW_OPS = {"sqrt", "div", "acos"}
+
+
+def slow_bound(L, fn):
+    """A bound function with a square root, a division or an arc cosine, or with 4 or more operations: the
+    batch kernel defers the cuboids whose propagation reaches one (they are evaluated afterwards on full
+    warps), so that the few lanes needing it do not hold up their warps."""
+    seen, ops = set(), []
+
+    def walk(nid):
+        if nid in seen:
+            return
+        seen.add(nid)
+        n = L.nodes[nid]
+        if n.op not in ("arg", "const", "bconst"):
+            ops.append(n.op)
+        for c in n.ch:
+            walk(c)
+
+    walk(fn)
+    return any(o in SLOW_OPS for o in ops) or len(ops) >= 4
+
+
 def tri_nn(n):
     return 1 if n.lb >= 0 else (0 if n.ub <= 0 else -1)
 
@@ -430,6 +453,8 @@ def generate(lemma):
     w("struct L {")
     w("    static constexpr int NARGS = %d;" % L.nargs)
     w("    static constexpr int NBOUNDS = %d;" % len(L.bounds))
+    w("    static constexpr std::uint64_t SLOW_BOUNDS = 0x%xull;   // bounds the batch kernel defers" %
+      mask(k for k, b in enumerate(L.bounds) if slow_bound(L, b[2])))
     for kind in ("lb", "ub", "both"):
         w("    __device__ __forceinline__ static std::uint64_t upd_%s(int a) {" % kind)
         w("        switch(a) {")

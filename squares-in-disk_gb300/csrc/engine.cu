@@ -982,6 +982,8 @@ struct sid_engine {
     DevBuf<double> batch_in_lo, batch_in_hi, batch_out_lo, batch_out_hi;
     DevBuf<std::int8_t> batch_verdict;
     DevBuf<std::uint32_t> batch_key, batch_order, batch_count, batch_totals;
+    DevBuf<std::uint64_t> batch_slow;             // deferred cuboids of a batch call (BatchArgs::slow)
+    DevBuf<unsigned long long> batch_slow_count;
     bool batch_profile = false;
     std::vector<cudaEvent_t> batch_events;   // four per profiled call: start, ordered, evaluated, scattered
     std::uint64_t batch_launches = 0;        // kernels launched by profiled calls
@@ -1084,7 +1086,14 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
         if(eng->batch_profile) eng->batch_launches += 5;
     }
     profile_mark(eng, s);
-    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order, stride, nullptr};
+    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order, stride, nullptr, nullptr, nullptr};
+    const bool defers = batch_defers(nargs);
+    if(defers) {
+        eng->batch_slow.reserve(std::size_t(n));
+        eng->batch_slow_count.reserve(1);
+        a.slow = eng->batch_slow.p;
+        a.slow_count = eng->batch_slow_count.p;
+    }
     const bool sample = !lem->batch_sample_pending && !lem->k->is_f32 && n > 0;
     if(sample) {
         if(!lem->batch_sample_host) {   // once per lemma: pinned (device-visible) host word, cleared counter
@@ -1097,7 +1106,7 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
         a.double_rows = lem->batch_sample.p;
     }
     cuda_check(lem->k->eval_batch(a, s), "eval batch");
-    if(eng->batch_profile) eng->batch_launches += n > 0 ? (sample ? 2 : 1) : 0;
+    if(eng->batch_profile) eng->batch_launches += n > 0 ? 1u + (defers ? 1u : 0u) + (sample ? 1u : 0u) : 0u;
     if(sample) {
         k_publish_sample<<<1, 1, 0, s>>>(lem->batch_sample.p, lem->batch_sample_host);
         cuda_check(cudaGetLastError(), "batch sample");

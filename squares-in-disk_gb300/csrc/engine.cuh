@@ -72,7 +72,7 @@ template<> __device__ __forceinline__ Iv<float> cst<float>(double, double, float
     return {flo, fhi, und};
 }
 
-template<class L, class T> __device__ bool propagate_packed(int arg, Iv<T>* box, int it_limit, int rec_limit);
+template<class L, class T, bool DEFER> __device__ int propagate_packed(int arg, Iv<T>* box, int it_limit, int rec_limit);
 
 /// Worklist bound propagation after a change of variable `arg` (both bounds), with the reference's
 /// FIFO order, de-duplication, per-bound recursion limit and "unstable" re-seeding between
@@ -81,7 +81,7 @@ template<class L, class T> __device__ bool propagate_packed(int arg, Iv<T>* box,
 template<class L, class T> __device__ bool propagate(int arg, Iv<T>* box, int it_limit, int rec_limit) {
     constexpr int NB = L::NBOUNDS;
     if(NB == 0) return false;
-    if constexpr(NB <= 16) return propagate_packed<L, T>(arg, box, it_limit, rec_limit);
+    if constexpr(NB <= 16) return propagate_packed<L, T, false>(arg, box, it_limit, rec_limit) == 1;
     const std::uint64_t seed = L::upd_both(arg);
     if(!seed) return false;
     std::uint8_t ring[NB > 0 ? NB : 1];
@@ -150,11 +150,12 @@ template<class L, class T> __device__ bool propagate(int arg, Iv<T>* box, int it
 /// the low nibble; a bound is queued at most once, so at most 16 entries), and the per-bound recursion
 /// counters are bytes of two 64-bit words (a counter grows only while below rec_limit <= 255, so it never
 /// carries into its neighbour). The byte arrays of the general form are indexed at run time and live in
-/// local memory.
-template<class L, class T> __device__ bool propagate_packed(int arg, Iv<T>* box, int it_limit, int rec_limit) {
+/// local memory. Returns 1 if the box became empty, else 0; with DEFER, 2 as soon as the next bound to
+/// apply is one of L::SLOW_BOUNDS (the box is then partly propagated, and the caller starts over elsewhere).
+template<class L, class T, bool DEFER> __device__ int propagate_packed(int arg, Iv<T>* box, int it_limit, int rec_limit) {
     static_assert(L::NBOUNDS <= 16, "packed worklist holds 16 bound ids");
     const std::uint64_t seed = L::upd_both(arg);
-    if(!seed) return false;
+    if(!seed) return 0;
     std::uint64_t q = 0, ul = 0, rec0 = 0, rec1 = 0;
     std::uint32_t present = 0, unstable = 0;
     int qn = 0, nun = 0;
@@ -167,11 +168,14 @@ template<class L, class T> __device__ bool propagate_packed(int arg, Iv<T>* box,
     for(int it = 0; it < it_limit; ++it) {
         while(qn > 0) {
             const int k = int(q & 15u);
+            if constexpr(DEFER) {
+                if((L::SLOW_BOUNDS >> k) & 1u) return 2;
+            }
             q >>= 4;
             --qn;
             present &= ~(1u << k);
             const int r = L::template apply_bound<T>(k, box);
-            if(r == B_EMPTY) return true;
+            if(r == B_EMPTY) return 1;
             if(r == B_NONE) continue;
             const int tgt = L::target(k);
             std::uint64_t upd = r == B_LB ? L::upd_lb(tgt) : (r == B_UB ? L::upd_ub(tgt) : L::upd_both(tgt));
@@ -210,7 +214,7 @@ template<class L, class T> __device__ bool propagate_packed(int arg, Iv<T>* box,
         ul = 0;
         nun = 0;
     }
-    return false;
+    return 0;
 }
 
 /// Splitter::subrange (splitter.hpp:44-59): width (ub-lb)/n and points lb + i*w, all rounded down
@@ -789,7 +793,36 @@ struct BatchArgs {
     const std::uint32_t* order;   // thread t evaluates cuboid order[t] (nullptr: cuboid t)
     std::uint64_t stride;         // distance between variables in lo/hi/out_lo/out_hi (0: n)
     unsigned long long* double_rows;   // if set: += cuboids whose constraints float could not refute
+    // deferred cuboids (both set, or neither): the evaluation kernel lists the cuboids whose propagation
+    // reaches one of L::SLOW_BOUNDS or whose constraints float cannot refute, and k_eval_batch_slow
+    // evaluates them on full warps; slow holds up to n cuboid indices, *slow_count is cleared per launch
+    std::uint64_t* slow;
+    unsigned long long* slow_count;
 };
+
+/// Whether the batch kernel of a lemma with `nargs` variables defers its rare expensive work (the bounds in
+/// L::SLOW_BOUNDS, the double constraints) to k_eval_batch_slow. Measured on 2^22-cuboid batches of every
+/// lemma: One Subcontainer 0.208 -> 0.167 ms, Top Packing 1 and 2 0.83 -> 0.77 and 1.07 -> 0.93 ms, Two
+/// and Four unchanged; for 5 or more variables the kernel that defers spills far more (>= 5 subcontainers,
+/// y_3 <= 0: 548 instead of 60 bytes of spill loads) and is slower (0.153 -> 0.199 ms), so they do not.
+/// The host passes the deferred list only to lemmas that use it.
+constexpr bool batch_defers(int nargs) { return nargs <= 4; }
+
+/// Deferred work stays in its warp when at least this many of the warp's lanes need it (they run it together
+/// with enough active lanes); fewer go to the deferred list.
+constexpr int kInlineLanes = 8;
+
+/// Appends the indices of the lanes with `want` to the batch's deferred list (one atomic per warp). Every
+/// lane of the warp calls it.
+__device__ __forceinline__ void defer_cuboids(const BatchArgs& a, bool want, std::uint64_t i) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if(!m) return;
+    const int leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if(int(lane_id()) == leader) base = atomicAdd(a.slow_count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if(want) a.slow[base + __popc(m & lanes_below())] = i;
+}
 
 /// Resident 128-thread blocks per SM the batch kernel is compiled for: 12 (42 registers) for lemmas with at
 /// most 3 variables, where the added warps hide more latency than the spills cost (One Subcontainer, 2^22
@@ -813,32 +846,60 @@ template<class L, class T> __device__ __noinline__ bool rows_ok_outlined(int r0,
 #define SID_BATCH_TILES 4           // 128-cuboid tiles per block of the batch kernel (1-16 measured, 4 fastest)
 #endif
 
-/// The second stage of the batch kernel for queue entry j: the cuboid's propagated box, which the first
-/// stage wrote, rounded outward to float; the constraints that compute, in float; then (double lemmas) all
-/// constraints in double for the cuboids float does not refute.
-template<class L, class T> __device__ __forceinline__ void batch_rest(const BatchArgs& a, std::uint64_t first,
-                                                                      const std::uint32_t* qpos, int j,
-                                                                      unsigned long long& n_double) {
+/// The second stage of the batch kernel for queue entry j (all lanes call it; `valid` marks the lanes with
+/// an entry): the cuboid's propagated box, which the first stage wrote, rounded outward to float; the
+/// constraints that compute, in float; then, for double lemmas and the cuboids float does not refute, all
+/// constraints in double, or with DEFER the cuboid goes to the deferred list.
+template<class L, class T, bool DEFER> __device__ __forceinline__ void batch_rest(const BatchArgs& a, std::uint64_t first,
+                                                                                  const std::uint32_t* qpos, int j,
+                                                                                  bool valid,
+                                                                                  unsigned long long& n_double) {
     constexpr int N = L::NARGS;
-    const std::uint64_t st = a.stride ? a.stride : a.n;
-    const std::uint64_t t = first + qpos[j];
-    const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
-    Iv<T> box[N];
-    Iv<float> fb[N];
-    #pragma unroll
-    for(int v = 0; v < N; ++v) {
-        box[v] = {T(a.out_lo[std::uint64_t(v) * st + i]), T(a.out_hi[std::uint64_t(v) * st + i]), false};
-        if constexpr(sizeof(T) == sizeof(double)) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
-        else fb[v] = {float(box[v].lo), float(box[v].hi), false};
+    bool defer = false;
+    std::uint64_t i = 0;
+    if(valid) {
+        const std::uint64_t st = a.stride ? a.stride : a.n;
+        const std::uint64_t t = first + qpos[j];
+        i = a.order ? std::uint64_t(a.order[t]) : t;
+        Iv<T> box[N];
+        Iv<float> fb[N];
+        #pragma unroll
+        for(int v = 0; v < N; ++v) {
+            box[v] = {T(a.out_lo[std::uint64_t(v) * st + i]), T(a.out_hi[std::uint64_t(v) * st + i]), false};
+            if constexpr(sizeof(T) == sizeof(double)) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
+            else fb[v] = {float(box[v].lo), float(box[v].hi), false};
+        }
+        std::int8_t vd = 0;
+        if(!L::template rows_rest<float>(N - 1, N, fb)) {
+            vd = 2;
+        } else if constexpr(sizeof(T) == sizeof(double)) {
+            if constexpr(DEFER) {
+                defer = true;
+            } else {
+                ++n_double;
+                if(!rows_ok_outlined<L, T>(N - 1, N, box)) vd = 2;
+            }
+        }
+        if(!defer) a.verdict[i] = vd;
     }
-    std::int8_t vd = 0;
-    if(!L::template rows_rest<float>(N - 1, N, fb)) {
-        vd = 2;
-    } else if constexpr(sizeof(T) == sizeof(double)) {
-        ++n_double;
-        if(!rows_ok_outlined<L, T>(N - 1, N, box)) vd = 2;
+    if constexpr(DEFER) {
+        // a few lanes whose constraints float cannot refute go to k_eval_batch_slow; when many of the warp's
+        // lanes need the double constraints, they test them here together instead
+        const unsigned dm = __ballot_sync(0xffffffffu, defer);
+        if(__popc(dm) >= kInlineLanes) {
+            if(defer) {
+                constexpr int N2 = L::NARGS;
+                const std::uint64_t st = a.stride ? a.stride : a.n;
+                Iv<T> box[N2];
+                #pragma unroll
+                for(int v = 0; v < N2; ++v) box[v] = {T(a.out_lo[std::uint64_t(v) * st + i]), T(a.out_hi[std::uint64_t(v) * st + i]), false};
+                ++n_double;
+                a.verdict[i] = rows_ok_outlined<L, T>(N2 - 1, N2, box) ? std::int8_t(0) : std::int8_t(2);
+            }
+            defer = false;
+        }
+        defer_cuboids(a, defer, i);
     }
-    a.verdict[i] = vd;
 }
 
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
@@ -855,7 +916,7 @@ template<class L, class T> __device__ __forceinline__ void batch_rest(const Batc
 /// constraints run on full warps instead of on the few lanes of every warp that need them. Threads follow
 /// `order` when given (the host orders tiles of 2^18 cuboids by the Morton code of the cuboids'
 /// positions); results go to each cuboid's own position.
-template<class L, class T> __global__ void __launch_bounds__(128, batch_min_blocks<L>()) k_eval_batch(const BatchArgs a) {
+template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, batch_min_blocks<L>()) k_eval_batch(const BatchArgs a) {
     constexpr int N = L::NARGS;
     constexpr int CAP = 256;
     __shared__ std::uint32_t qpos[CAP];
@@ -870,14 +931,38 @@ template<class L, class T> __global__ void __launch_bounds__(128, batch_min_bloc
         const std::uint64_t base = first + std::uint64_t(tile) * 128u;
         if(base >= a.n) break;                                  // uniform over the block
         const std::uint64_t t = base + threadIdx.x;
-        bool push = false;
-        if(t < a.n) {
-            const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
-            Iv<T> box[N];
+        const bool valid = t < a.n;
+        bool push = false, defer = false;
+        std::uint64_t i = 0;
+        Iv<T> box[N];
+        int pr = 0;
+        if(valid) {
+            i = a.order ? std::uint64_t(a.order[t]) : t;
             #pragma unroll
             for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
+            if constexpr(DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0) {
+                pr = propagate_packed<L, T, true>(N - 1, box, N, 4);
+            } else {
+                pr = propagate<L, T>(N - 1, box, N, 4) ? 1 : 0;
+            }
+        }
+        if constexpr(DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0) {
+            // a few lanes that reached a slow bound go to k_eval_batch_slow; when many of the warp's lanes
+            // did, they start over here together instead
+            const unsigned dm = __ballot_sync(0xffffffffu, pr == 2);
+            if(__popc(dm) >= kInlineLanes) {
+                if(pr == 2) {
+                    #pragma unroll
+                    for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
+                    pr = propagate<L, T>(N - 1, box, N, 4) ? 1 : 0;
+                }
+            } else {
+                defer = pr == 2;
+            }
+        }
+        if(valid && !defer) {
             std::int8_t vd = 0;
-            if(propagate<L, T>(N - 1, box, N, 4)) {
+            if(pr == 1) {
                 vd = 1;
             } else if(!L::template rows_cheap<T>(N - 1, N, box)) {
                 vd = 2;
@@ -891,6 +976,7 @@ template<class L, class T> __global__ void __launch_bounds__(128, batch_min_bloc
                 a.out_hi[std::uint64_t(v) * st + i] = double(box[v].hi);
             }
         }
+        if constexpr(DEFER) defer_cuboids(a, defer, i);
         const unsigned m = __ballot_sync(0xffffffffu, push);
         if(m) {
             int at = 0;
@@ -902,7 +988,7 @@ template<class L, class T> __global__ void __launch_bounds__(128, batch_min_bloc
         const int q = qn;
         __syncthreads();                                        // every warp has read qn before the next tile appends
         if(q >= 128) {
-            batch_rest<L, T>(a, first, qpos, int(threadIdx.x), n_double);
+            batch_rest<L, T, DEFER>(a, first, qpos, int(threadIdx.x), true, n_double);
             __syncthreads();
             const int j = int(threadIdx.x) + 128;
             if(j < q) qpos[threadIdx.x] = qpos[j];
@@ -911,7 +997,55 @@ template<class L, class T> __global__ void __launch_bounds__(128, batch_min_bloc
         }
     }
     const int q = qn;
-    if(int(threadIdx.x) < q) batch_rest<L, T>(a, first, qpos, int(threadIdx.x), n_double);
+    if(q > 0) batch_rest<L, T, DEFER>(a, first, qpos, int(threadIdx.x), int(threadIdx.x) < q, n_double);
+    if(a.double_rows) {
+        const unsigned long long w = __reduce_add_sync(0xffffffffu, unsigned(n_double));
+        if(lane_id() == 0 && w) atomicAdd(a.double_rows, w);
+    }
+}
+
+/// The deferred cuboids of a batch (BatchArgs::slow, *slow_count of them), one per thread on full warps:
+/// each is evaluated from its input box exactly as the first and second stage of k_eval_batch would have
+/// (propagation with every bound, the comparison-only constraints in double, the others in float and in
+/// double where float does not refute), so its outputs are those of the undeferred evaluation bit for bit.
+template<class L, class T> __global__ void __launch_bounds__(128, 8) k_eval_batch_slow(const BatchArgs a) {
+    constexpr int N = L::NARGS;
+    const std::uint64_t n = *a.slow_count;
+    const std::uint64_t st = a.stride ? a.stride : a.n;
+    const bool rest = L::has_rest(N - 1, N);
+    unsigned long long n_double = 0;
+    for(std::uint64_t j = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n;
+        j += std::uint64_t(gridDim.x) * blockDim.x) {
+        const std::uint64_t i = a.slow[j];
+        Iv<T> box[N];
+        #pragma unroll
+        for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
+        std::int8_t vd = 0;
+        if(propagate<L, T>(N - 1, box, N, 4)) {
+            vd = 1;
+        } else if(!L::template rows_cheap<T>(N - 1, N, box)) {
+            vd = 2;
+        } else if(rest) {
+            Iv<float> fb[N];
+            #pragma unroll
+            for(int v = 0; v < N; ++v) {
+                if constexpr(sizeof(T) == sizeof(double)) fb[v] = {__double2float_rd(box[v].lo), __double2float_ru(box[v].hi), false};
+                else fb[v] = {float(box[v].lo), float(box[v].hi), false};
+            }
+            if(!L::template rows_rest<float>(N - 1, N, fb)) {
+                vd = 2;
+            } else if constexpr(sizeof(T) == sizeof(double)) {
+                ++n_double;
+                if(!rows_ok_outlined<L, T>(N - 1, N, box)) vd = 2;
+            }
+        }
+        a.verdict[i] = vd;
+        #pragma unroll
+        for(int v = 0; v < N; ++v) {
+            a.out_lo[std::uint64_t(v) * st + i] = double(box[v].lo);
+            a.out_hi[std::uint64_t(v) * st + i] = double(box[v].hi);
+        }
+    }
     if(a.double_rows) {
         const unsigned long long w = __reduce_add_sync(0xffffffffu, unsigned(n_double));
         if(lane_id() == 0 && w) atomicAdd(a.double_rows, w);
@@ -1003,7 +1137,20 @@ template<class L, class T> cudaError_t launch_eval_batch(const BatchArgs& a, cud
     const unsigned threads = 128;
     const std::uint64_t per_block = std::uint64_t(threads) * SID_BATCH_TILES;
     const std::uint64_t blocks = (a.n + per_block - 1) / per_block;
-    k_eval_batch<L, T><<<unsigned(blocks), threads, 0, s>>>(a);
+    if constexpr(batch_defers(L::NARGS)) {
+        if(a.slow) {
+            const cudaError_t e = cudaMemsetAsync(a.slow_count, 0, sizeof(unsigned long long), s);
+            if(e != cudaSuccess) return e;
+            k_eval_batch<L, T, true><<<unsigned(blocks), threads, 0, s>>>(a);
+            // grid-stride over the deferred list, whose length only the device knows: enough blocks to fill
+            // the GPU
+            const std::uint64_t want_blocks = (a.n + threads - 1) / threads;
+            const std::uint64_t slow_blocks = want_blocks < 152u * 8u ? want_blocks : 152u * 8u;
+            k_eval_batch_slow<L, T><<<unsigned(slow_blocks), threads, 0, s>>>(a);
+            return cudaGetLastError();
+        }
+    }
+    k_eval_batch<L, T, false><<<unsigned(blocks), threads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
