@@ -913,9 +913,12 @@ template<class L, class T, bool DEFER> __device__ __forceinline__ void batch_res
 /// tests the constraints that compute in float (every float interval contains the double interval of the
 /// same node, so a float refutation is the double one), and in double where float does not refute. Few
 /// cuboids reach stage 2 (~10 % of One Subcontainer's synthetic batch), so the conversions and the float
-/// constraints run on full warps instead of on the few lanes of every warp that need them. Threads follow
-/// `order` when given (the host orders tiles of 2^18 cuboids by the Morton code of the cuboids'
-/// positions); results go to each cuboid's own position.
+/// constraints run on full warps instead of on the few lanes of every warp that need them. With DEFER
+/// (lemmas for which batch_defers holds, given the deferred list), rarer and costlier work leaves the warp
+/// too: a cuboid whose propagation reaches one of L::SLOW_BOUNDS, or whose constraints float cannot refute,
+/// goes to the deferred list unless kInlineLanes lanes of its warp need the same, and k_eval_batch_slow
+/// evaluates the list afterwards. Threads follow `order` when given (the host orders tiles of 2^18 cuboids
+/// by the Morton code of the cuboids' positions); results go to each cuboid's own position.
 template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, batch_min_blocks<L>()) k_eval_batch(const BatchArgs a) {
     constexpr int N = L::NARGS;
     constexpr int CAP = 256;
