@@ -809,8 +809,12 @@ struct BatchArgs {
 constexpr bool batch_defers(int nargs) { return nargs <= 4; }
 
 /// Deferred work stays in its warp when at least this many of the warp's lanes need it (they run it together
-/// with enough active lanes); fewer go to the deferred list.
+/// with enough active lanes); fewer go to the deferred list. Only for lemmas of at most 2 variables: the
+/// code that re-runs the work in place raises the kernel's register pressure, which costs the others more
+/// (One Subcontainer, 2^24 cuboids: 0.540 ms without it, 0.563 with it) than it saves them, while the Top
+/// Packing lemmas, whose slow bound many lanes reach, gain (2^22 cuboids: 1.22 -> 0.93 ms).
 constexpr int kInlineLanes = 8;
+__host__ __device__ constexpr bool batch_inline(int nargs) { return nargs <= 2; }
 
 /// Appends the indices of the lanes with `want` to the batch's deferred list (one atomic per warp). Every
 /// lane of the warp calls it.
@@ -885,7 +889,7 @@ template<class L, class T, bool DEFER> __device__ __forceinline__ void batch_res
     if constexpr(DEFER) {
         // a few lanes whose constraints float cannot refute go to k_eval_batch_slow; when many of the warp's
         // lanes need the double constraints, they test them here together instead
-        const unsigned dm = __ballot_sync(0xffffffffu, defer);
+        const unsigned dm = batch_inline(L::NARGS) ? __ballot_sync(0xffffffffu, defer) : 0u;
         if(__popc(dm) >= kInlineLanes) {
             if(defer) {
                 constexpr int N2 = L::NARGS;
@@ -949,7 +953,9 @@ template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, ba
                 pr = propagate<L, T>(N - 1, box, N, 4) ? 1 : 0;
             }
         }
-        if constexpr(DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0) {
+        if constexpr(DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0 && !batch_inline(L::NARGS)) {
+            defer = pr == 2;
+        } else if constexpr(DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0) {
             // a few lanes that reached a slow bound go to k_eval_batch_slow; when many of the warp's lanes
             // did, they start over here together instead
             const unsigned dm = __ballot_sync(0xffffffffu, pr == 2);
