@@ -828,15 +828,16 @@ __device__ __forceinline__ void defer_cuboids(const BatchArgs& a, bool want, std
     if(want) a.slow[base + __popc(m & lanes_below())] = i;
 }
 
-/// Resident 128-thread blocks per SM the batch kernel is compiled for: 12 (42 registers) for lemmas with at
-/// most 3 variables, where the added warps hide more latency than the spills cost (One Subcontainer, 2^22
-/// cuboids: 0.225 -> 0.207 ms), 8 (64 registers) above (Four Subcontainer 0.174 ms at 8, 0.197 at 12).
-/// SID_BATCH_MIN_BLOCKS overrides it for tuning builds.
+/// Resident 128-thread blocks per SM the batch kernel is compiled for: 10 (48 registers) for lemmas with at
+/// most 3 variables, where the added warps hide more latency than the spills cost (One Subcontainer, 2^24
+/// cuboids, with deferred work: 8 blocks 0.507 ms, 9 0.507, 10 0.496, 12 0.540, 14 and 16 0.560), 8 (64
+/// registers) above (Two Subcontainer, 2^22 cuboids: 0.170 ms at 8, 0.180 at 10; >= 5 subcontainers 3-4 %
+/// slower at 10). SID_BATCH_MIN_BLOCKS overrides it for tuning builds.
 template<class L> constexpr int batch_min_blocks() {
 #ifdef SID_BATCH_MIN_BLOCKS
     return SID_BATCH_MIN_BLOCKS;
 #else
-    return L::NARGS <= 3 ? 12 : 8;
+    return L::NARGS <= 3 ? 10 : 8;
 #endif
 }
 
