@@ -43,8 +43,8 @@ SEED = 0x5EED0001
 BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
 # DRAM bytes (read + write) of one evaluation on this workload (k_eval_batch and k_eval_batch_slow), from ncu
 # (profiles/k_eval_batch_one_subcontainer_2e24.md); traffic grows in proportion to the batch
-NCU_TRAFFIC_BYTES_2E24 = 0.901654e9 + 0.833207e9 + 0.046650e9 + 0.009055e9
-NCU_FP64_PIPE_ACTIVE = 0.523
+NCU_TRAFFIC_BYTES_2E24 = 0.846948e9 + 0.789978e9 + 0.046737e9 + 0.009150e9
+NCU_FP64_PIPE_ACTIVE = 0.579
 # FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
 FP64_LANES_PER_CLOCK = 304
 # FP32 lanes per clock of the whole GPU: 152 SMs x 128
@@ -466,9 +466,9 @@ def run_ours(args):
                      "kernel": "k_eval_batch + k_eval_batch_slow (one_subcontainer, two stages, deferred cuboids, adaptive order)",
                      "kernel_ms": kernel_s * 1000.0, "ordering_ms_per_step": order_ms / max(prof_calls, 1),
                      "note": "algorithmic bytes (97 per cuboid) over the event-timed evaluation (both kernels); "
-                             "DRAM traffic is 10 % above them (stage 2 and the deferred kernel re-read boxes, "
-                             "spills); the main kernel issues on 59 % of cycles with its FP64 pipe 52 % busy "
-                             "and DRAM 48 %, so it is bound by instruction issue and latency, not by HBM "
+                             "DRAM traffic is 4 % above them (the deferred kernel re-reads its cuboids); the "
+                             "main kernel issues on 62 % of cycles with its FP64 pipe 58 % busy and DRAM 50 %, "
+                             "so it is bound by instruction issue and latency, not by HBM "
                              "(profiles/k_eval_batch_one_subcontainer_2e24.md)"},
         "gpu_launches": launches,
         "clocks": clk,
