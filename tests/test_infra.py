@@ -41,6 +41,22 @@ def test_codegen_runs_on_all_ir(tmp_path):
     assert (tmp_path / "registry.cu").exists()
 
 
+def test_slow_bounds_are_the_costly_bound_functions():
+    """The batch kernel defers cuboids whose propagation reaches a slow bound. One Subcontainer's slow bounds
+    are 7 and 10 (a square root, and two square roots with a division); a bound that only copies a
+    variable's or a constant's range is never slow."""
+    sys.path.insert(0, os.path.join(sid.PKG, "csrc"))
+    import codegen
+    L = codegen.Lemma(os.path.join(sid.LEMMA_DIR, "one_subcontainer.sidir"))
+    slow = [k for k, b in enumerate(L.bounds) if codegen.slow_bound(L, b[2])]
+    assert slow == [7, 10]
+    for name in sid.lemma_names():
+        L = codegen.Lemma(os.path.join(sid.LEMMA_DIR, name + ".sidir"))
+        for tgt, d, fn, defined in L.bounds:
+            if L.nodes[fn].op in ("arg", "const"):
+                assert not codegen.slow_bound(L, fn), (name, fn)
+
+
 def test_fingerprints_match_cpp_and_python():
     sys.path.insert(0, os.path.join(sid.PKG, "csrc"))
     import codegen
