@@ -41,8 +41,9 @@ N_CUBOIDS = 1 << 24
 SEED = 0x5EED0001
 # algorithmic bytes per cuboid of the batch kernel: read 2*8*nargs, write 2*8*nargs + 1 verdict byte
 BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
-# DRAM bytes (read + write) of one evaluation on this workload (k_eval_batch and k_eval_batch_slow), from ncu
-# (profiles/k_eval_batch_one_subcontainer_2e24.md); traffic grows in proportion to the batch
+# DRAM bytes (read + write) of one evaluation on this workload (k_eval_batch and k_eval_batch_slow), from an ncu
+# capture of the same kernels on the same batch (dram__bytes_read.sum + dram__bytes_write.sum); traffic grows in
+# proportion to the batch
 NCU_TRAFFIC_BYTES_2E24 = 0.846948e9 + 0.789978e9 + 0.046737e9 + 0.009150e9
 NCU_FP64_PIPE_ACTIVE = 0.579
 # FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
@@ -50,6 +51,7 @@ FP64_LANES_PER_CLOCK = 304
 # FP32 lanes per clock of the whole GPU: 152 SMs x 128
 FP32_LANES_PER_CLOCK = 19456
 OPS_TABLE = os.path.join(REPO, "tests", "golden", "ops_per_cuboid.json")
+CLOCK_WINDOW_S = 0.6   # seconds of load the clock sampler sees after the timed steps
 
 
 def measured_peaks():
@@ -76,7 +78,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -145,21 +147,21 @@ def whole_job_rate(units_per_rank, world, seconds):
     return units_per_rank * world / seconds
 
 
-def cpu_baseline(ir, lo, hi, threads, budget_s=1.5):
-    """Time the CPU oracle on a bounded prefix of the batch with `threads` host threads."""
+def cpu_baseline(ir, lo, hi, threads, cpu_seconds=16.0):
+    """Time the CPU oracle with `threads` host threads on a bounded sample of the batch: whole passes over the
+    batch's first cuboids (up to 2^22 of them), as many as make about cpu_seconds of CPU work (thread-seconds),
+    after one untimed pass. Returns (cuboids evaluated, wall seconds)."""
     import oracle_py
     oracle_py.build()
-    n = lo.shape[1]
-    sample = min(n, 1 << 18)
+    sample = min(lo.shape[1], 1 << 22)
     t0 = time.perf_counter()
     oracle_py.eval_batch(ir, lo[:, :sample], hi[:, :sample], threads=threads)
-    dt = time.perf_counter() - t0
-    # grow the sample to roughly budget_s of wall time (10-30 s of CPU work on all cores)
-    sample = int(min(n, max(sample, sample * budget_s / max(dt, 1e-6))))
+    dt = max(time.perf_counter() - t0, 1e-6)
+    passes = max(1, int(round(cpu_seconds / max(threads, 1) / dt)))
     t0 = time.perf_counter()
-    oracle_py.eval_batch(ir, lo[:, :sample], hi[:, :sample], threads=threads)
-    dt = time.perf_counter() - t0
-    return sample, dt
+    for _ in range(passes):
+        oracle_py.eval_batch(ir, lo[:, :sample], hi[:, :sample], threads=threads)
+    return sample * passes, time.perf_counter() - t0
 
 
 PRECISION_PLAIN, PRECISION_FP32, PRECISION_TUNED = 0, 1, 2
@@ -351,6 +353,45 @@ def run_reference(args):
     return 0
 
 
+def plain_fp64_leg(eng, lid, d_lo, d_hi, o_lo, o_hi, o_v, n, nargs, stream, args):
+    """sid_eval_batch_plain_device on the benchmark's batch: CUDA events around each call's evaluation kernel
+    (on the launching stream), the same warm-up and step count as the headline; outputs compared bit for bit
+    with the float-first kernel's (o_lo, o_hi, o_v hold those)."""
+    import torch
+    ref_lo, ref_hi, ref_v = o_lo.clone(), o_hi.clone(), o_v.clone()
+    p_lo, p_hi = torch.empty_like(o_lo), torch.empty_like(o_hi)
+    p_v = torch.empty_like(o_v)
+
+    def step():
+        eng.eval_batch_plain_device(lid, d_lo.data_ptr(), d_hi.data_ptr(), n, p_lo.data_ptr(), p_hi.data_ptr(),
+                                    p_v.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    eng.batch_profile(True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    calls, order_ms, eval_ms = eng.batch_profile_read()
+    eng.batch_profile(False)
+    same = bool(torch.equal(p_v, ref_v) and torch.equal(p_lo.view(torch.int64), ref_lo.view(torch.int64)) and
+                torch.equal(p_hi.view(torch.int64), ref_hi.view(torch.int64)))
+    kernel_s = eval_ms / 1000.0 / max(calls, 1)
+    with open(OPS_TABLE) as f:
+        ops = json.load(f)["batch_plain"][LEMMA]["total"]
+    return {"value": n * args.steps / (ms / 1000.0), "unit": "cuboids/s", "ms_per_step": ms / args.steps,
+            "kernel": "k_eval_batch_plain (the reference's order in double, Morton order within tiles of 2^18)",
+            "kernel_ms": kernel_s * 1000.0, "ordering_ms_per_step": order_ms / max(calls, 1),
+            "ops_per_cuboid": ops, "hbm_gbs": BYTES_PER_CUBOID(nargs) * n / kernel_s / 1e9,
+            "outputs_equal_float_first_kernel": same}
+
+
 def run_ours(args):
     import torch
     import sid_gb300 as sid
@@ -397,13 +438,24 @@ def run_ours(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
-    clk = clocks.stop()
     prof_calls, order_ms, eval_ms, launches = eng.batch_profile_read(with_launches=True)
     eng.batch_profile(False)
+    # the timed steps take milliseconds, shorter than the sampler's period: the same step keeps running, untimed,
+    # until the sampler has seen CLOCK_WINDOW_S of load, so the clock record reflects this workload
+    t_end = time.perf_counter() + CLOCK_WINDOW_S
+    while time.perf_counter() < t_end:
+        for _ in range(20):
+            step()
+        torch.cuda.synchronize()
+    clk = clocks.stop()
+    clk["window"] = "the timed steps, then %.1f s of the same steps untimed" % CLOCK_WINDOW_S
     ms = max_over_ranks(dist, ms)
     if dist:
         dist.barrier()
     value = whole_job_rate(n * args.steps, world, ms / 1000.0)
+
+    # the all-double kernel (the reference's order, no float test) on the same batch: the FP64 baseline
+    plain = plain_fp64_leg(eng, lid, d_lo, d_hi, o_lo, o_hi, o_v, n, nargs, stream, args)
 
     # end to end through the C ABI with pinned host buffers
     h_lo = torch.from_numpy(lo).pin_memory()
@@ -468,8 +520,7 @@ def run_ours(args):
                      "note": "algorithmic bytes (97 per cuboid) over the event-timed evaluation (both kernels); "
                              "DRAM traffic is 4 % above them (the deferred kernel re-reads its cuboids); the "
                              "main kernel issues on 62 % of cycles with its FP64 pipe 58 % busy and DRAM 50 %, "
-                             "so it is bound by instruction issue and latency, not by HBM "
-                             "(profiles/k_eval_batch_one_subcontainer_2e24.md)"},
+                             "so it is bound by instruction issue and latency, not by HBM (ncu)"},
         "gpu_launches": launches,
         "clocks": clk,
         "proof": {"lemma": LEMMA, "cuboids": best["cuboids"], "leaves": best["leaves"],
@@ -499,6 +550,11 @@ def run_ours(args):
         "frac": achieved_f32 / peak_f32,
         "note": "directed-rounding float operations per cuboid of the float constraint test, same table and "
                 "kernel time, against one FP32 instruction per lane and clock"}
+    plain["fp64_ops_achieved"] = plain["ops_per_cuboid"] * n / (plain["kernel_ms"] / 1000.0) / 1e9
+    plain["fp64_ops_peak"] = peak_gops
+    plain["fp64_ops_frac"] = plain["fp64_ops_achieved"] / peak_gops
+    plain["hbm_frac"] = plain["hbm_gbs"] / peak
+    line["plain_fp64"] = plain
     if lemma_set:
         line["lemma_set"] = lemma_set
     if serve:
@@ -509,7 +565,8 @@ def run_ours(args):
         threads = os.cpu_count() or 1
         sample, dt = cpu_baseline(ir, lo, hi, threads)
         line["cpu_baseline"] = {"value": sample / dt, "unit": "cuboids/s", "cores": threads, "kind": "port",
-                                "sample": "first %d cuboids of the batch, %.2f s wall" % (sample, dt)}
+                                "sample": "%d cuboids (whole passes over the batch's first 2^22 cuboids), %.2f s wall"
+                                          % (sample, dt)}
     print(json.dumps(line))
     eng.close()
     if dist:

@@ -76,9 +76,15 @@ typedef void (*sid_progress_fn)(void* user, const sid_progress* progress);
 /* Settings of one proof; meaning as ivarp::ProverSettings (prover_input.hpp:124-159). */
 typedef struct sid_prove_opts {
     uint32_t generation_count;          /* default 8 */
-    int32_t max_iterations_per_node;    /* <= 1: no re-iteration (the published proofs use 1) */
-    float iteration_volume_criterion;
-    float iteration_single_dimension_criterion;
+    int32_t max_iterations_per_node;    /* passes over the static splits per queue element (p_handle_cuboid_nf,
+                                           cpu_prover_core.hpp:113-134): after a pass, the hull of the surviving
+                                           leaves is run again as the element while fewer than this many passes
+                                           ran and a criterion below accepts it, each repeat counting one cuboid
+                                           and one repeated node; <= 1: one pass (the published proofs use 1) */
+    float iteration_volume_criterion;   /* repeat if the hull's volume exceeds this share of the element's */
+    float iteration_single_dimension_criterion;   /* repeat if some variable's hull width exceeds this share of
+                                                     the element's width (both in the lemma's number type,
+                                                     rounded down as the reference computes them) */
     int64_t batch_elements;             /* queue elements expanded per step; <= 0: engine default */
     int32_t precision;                  /* SID_PRECISION_* */
     uint64_t max_criticals_kept;        /* criticals stored for sid_fetch_criticals */
@@ -186,6 +192,30 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
 int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
                           double* out_lo, double* out_hi, int8_t* verdict, void* stream);
 
+/* The all-double form of sid_eval_batch_device: the same outputs bit for bit, computed in the reference's
+ * order only (cpu_prover_core.hpp:221-256 at the innermost level: propagation, then the last row's constraints
+ * in double, stopping at the first violated one), without the float test of the constraints. Always evaluated
+ * in the Morton order of the cuboids' lower corners within tiles of 2^18 cuboids (ordering scratch of the
+ * engine, as sid_eval_batch_device). It is the FP64 baseline the float-first kernel is measured against. */
+int sid_eval_batch_plain_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
+                                double* out_lo, double* out_hi, int8_t* verdict, void* stream);
+
+/* Interval endpoints of the lemma's criteria (no counterpart in the reference, whose constraint evaluation
+ * keeps them internal: runtime_constraint_table.hpp:31-115 evaluates each constraint's comparisons and keeps
+ * only the verdict). The lemma's constraints compare pairs of expressions; sid_lemma_operands gives the number
+ * of compared expressions K: constraints in table order, each constraint's predicate tree in pre-order, the
+ * left and the right operand of every comparison not decided at compile time, each comparison once.
+ * sid_eval_operands_device evaluates all K expressions on each of n boxes (device buffers, structure of
+ * arrays lo[v*n + i], hi[v*n + i]; pass a propagated box from sid_eval_batch_device to get the values the
+ * constraints saw): use_float 0 in the lemma's own number type (double: the plain form's endpoints), 1 in
+ * float on the box rounded outward (the precision form's first pass). Outputs (device): out_lohi[2*(j*n + i)]
+ * and [2*(j*n + i) + 1] the lower and upper endpoint of expression j on box i, out_undefined[j*n + i] 1 if the
+ * value is possibly undefined (e.g. a square root of a possibly negative argument), else 0. Every expression
+ * is evaluated whether or not an earlier constraint already failed. Asynchronous on `stream`. */
+int sid_lemma_operands(sid_engine* engine, int lemma_id, uint32_t* count);
+int sid_eval_operands_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
+                             int use_float, double* out_lohi, int8_t* out_undefined, void* stream);
+
 /* Kernel timing of the batch calls, for roofline measurements (no counterpart in the reference).
  * sid_eval_batch_profile(engine, 1) makes every following sid_eval_batch* call record CUDA events on its
  * stream around its evaluation kernel and around its ordering kernel; sid_eval_batch_profile_read waits
@@ -216,22 +246,34 @@ int sid_lemma_batch_order(sid_engine* engine, int lemma_id, int mode, double* do
  * budget and must not call the allocator (which can block, fragment memory or synchronize the device)
  * on every request, or a host application that owns all device memory through its own pool and does
  * not let third-party code call cudaMalloc. This call allocates nothing: no cudaMalloc or cudaFree and
- * no other allocating routine, on the host or on the device.
+ * no other allocating routine, on the host or on the device. Double lemmas only (SID_ERR_UNSUPPORTED for float lemmas).
  *
  * For each of the n parent cuboids in `boxes`, split the lemma's last static variable into its
  * configured number of pieces, propagate bounds and test the constraints (the innermost step of the
  * prover core), and join the surviving pieces into that parent's hull. Layout of `boxes` and `hulls`
  * (device memory): (lo, hi) pairs, variable-major: pair [v*n + i]. nonempty[i] (device) is 1 if any
  * piece of parent i survived, else 0 and hulls for i are left untouched; *leaves (device, may be NULL)
- * receives the number of leaves (every piece is a leaf). Asynchronous on `stream` (a cudaStream_t).
+ * receives the number of leaves (every piece is a leaf; 0 when n is 0). Asynchronous on `stream` (a
+ * cudaStream_t).
  *
  * Its working memory is one 8 MiB array per device inside libsid.so, held from library load until the
  * process exits; n * nargs must be at most 262,136 (larger calls fail with SID_ERR_CAPACITY). The first
- * call on a device looks up that array's device address; make this first call before any stream
- * capture. All calls on a device share the array: calls whose work overlaps on the GPU (different
+ * call on a device looks up that array's device address and keeps it for the life of the process: make this
+ * first call before any stream capture, and do not reset the device (cudaDeviceReset) after it. All calls on a device share the array: calls whose work overlaps on the GPU (different
  * streams or host threads) race and corrupt each other's results, so serialize them. */
 int sid_leaf_hull_noalloc(sid_engine* engine, int lemma_id, const double* boxes, uint64_t n, double* hulls,
                           uint8_t* nonempty, unsigned long long* leaves, void* stream);
+
+/* Host-side fault injection, for tests of the error paths (no counterpart in the reference, whose worker
+ * errors are rethrown on the caller's thread, proof_driver.hpp:99-118). Arms a countdown in this process: the
+ * countdown-th following device allocation of an engine (SID_INJECT_ALLOC) or kernel launch of the proof,
+ * served and batch paths (SID_INJECT_LAUNCH) fails as if CUDA had returned cudaErrorMemoryAllocation or
+ * cudaErrorLaunchFailure, without allocating or launching anything, and the call that meets it returns
+ * SID_ERR_NOMEM or SID_ERR_CUDA (a served request: SID_REQ_FAILED). The engine and its servers stay usable
+ * afterwards. countdown 0 disarms; an injection fires once. Nothing is injected on the GPU. */
+#define SID_INJECT_ALLOC 1
+#define SID_INJECT_LAUNCH 2
+int sid_debug_inject_failure(int kind, int64_t countdown);
 
 /* ---- Served form: a request loop with continuous batching. No counterpart in the reference (its
  * driver proves one lemma per run_prover call); an addition of this library for proving many lemmas
@@ -255,12 +297,17 @@ typedef struct sid_server_opts {
     uint32_t generation_count;          /* generations per request; 0: 8 */
     uint64_t max_criticals_per_request; /* critical boxes stored per request */
     uint32_t max_requests_per_lane;     /* admitted at once per lemma; 0: 1024 */
+    int32_t max_iterations_per_node;    /* node re-iteration as in sid_prove_opts; default 1 (none) */
+    float iteration_volume_criterion;   /* default 0.25 */
+    float iteration_single_dimension_criterion;   /* default 0.66 */
 } sid_server_opts;
 
 #define SID_REQ_PENDING 0                /* waiting for admission */
 #define SID_REQ_RUNNING 1
 #define SID_REQ_DONE 2
-#define SID_REQ_FAILED 3                 /* see sid_last_error() after sid_request_poll/wait */
+#define SID_REQ_FAILED 3                 /* sid_request_poll/wait then fill the status and return the failure's
+                                            own status (e.g. SID_ERR_NOMEM, SID_ERR_CUDA); sid_last_error() says
+                                            what failed. The server keeps serving other requests. */
 
 typedef struct sid_request_status {
     int32_t state;                      /* SID_REQ_* */
@@ -272,6 +319,7 @@ typedef struct sid_request_status {
     uint64_t criticals_stored;
     double seconds_queued;              /* submission to admission */
     double seconds_to_verdict;          /* submission to completion (host clock) */
+    uint64_t num_repeated_nodes;        /* nodes re-iterated on their hull */
 } sid_request_status;
 
 void sid_server_opts_default(sid_server_opts* opts);

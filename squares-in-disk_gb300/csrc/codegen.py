@@ -136,6 +136,28 @@ def slow_bound(L, fn):
     return any(o in SLOW_OPS for o in ops) or len(ops) >= 4
 
 
+def comparison_operands(L):
+    """The expressions compared by the constraints' comparison nodes that are not decided at compile time, in
+    the oracle's order (oracle/oracle.cpp, comparison_operands): constraints in table order, each predicate tree
+    in pre-order, (left, right) per comparison, every comparison node once."""
+    out, seen = [], set()
+    for root in L.constraints:
+        stack = [root]
+        while stack:
+            nid = stack.pop()
+            if nid in seen:
+                continue
+            seen.add(nid)
+            n = L.nodes[nid]
+            if n.lb == n.ub:
+                continue
+            if n.op in CMP_OPS:
+                out += [n.ch[0], n.ch[1]]
+            elif n.op in ("orseq", "andseq", "or", "and", "not"):
+                stack.extend(reversed(n.ch))
+    return out
+
+
 def tri_nn(n):
     return 1 if n.lb >= 0 else (0 if n.ub <= 0 else -1)
 
@@ -502,6 +524,11 @@ def generate(lemma):
     for r in range(L.nargs):
         w("    template<class T> __device__ static bool rowc_%d(const Iv<T>* box);" % r)
         w("    template<class T> __device__ static bool rowx_%d(const Iv<T>* box);" % r)
+    operands = comparison_operands(L)
+    w("    // the expressions the constraints compare (left, right per comparison), for endpoint dumps")
+    w("    static constexpr int NOPERANDS = %d;" % len(operands))
+    w("    template<class T> __device__ static void operands(const Iv<T>* box, double2* out, std::int8_t* und,")
+    w("                                                      std::uint64_t stride, std::uint64_t i);")
     w("};")
     w("")
     # bound functions
@@ -575,6 +602,18 @@ def generate(lemma):
     w("    return status;")
     w("}")
     w("")
+    w("template<class T> __device__ void L::operands(const Iv<T>* box, double2* out, std::int8_t* und,")
+    w("                                              std::uint64_t stride, std::uint64_t i) {")
+    e = Emitter(L)
+    scope = {}
+    for j, nid in enumerate(operands):
+        x = e.expr(nid, scope)
+        e.emit("out[%d * stride + i] = make_double2(double(%s.lo), double(%s.hi));" % (j, x, x))
+        e.emit("und[%d * stride + i] = %s.und ? 1 : 0;" % (j, x))
+    out.extend(e.lines)
+    w("    (void)box; (void)out; (void)und; (void)stride; (void)i;")
+    w("}")
+    w("")
     hoisted = []
     if L.numtype != "f32":
         w("template<int LV> struct H;")
@@ -609,6 +648,13 @@ def generate(lemma):
     w("static cudaError_t level(int mode, const LevelArgs& a, cudaStream_t s) { return launch_level<L, %s>(mode, a, s); }" % T_plain)
     w("static cudaError_t root_box(double2* o, cudaStream_t s) { return launch_root_box<L, %s>(o, s); }" % T_plain)
     w("static cudaError_t eval_batch(const BatchArgs& a, cudaStream_t s) { return launch_eval_batch<L, %s>(a, s); }" % T_plain)
+    w("static cudaError_t eval_batch_plain(const BatchArgs& a, cudaStream_t s) {")
+    w("    return launch_eval_batch_plain<L, %s>(a, s);" % T_plain)
+    w("}")
+    w("static cudaError_t eval_operands(int use_float, const double* lo, const double* hi, std::uint64_t n,")
+    w("                                 std::uint64_t stride, double2* o, std::int8_t* u, cudaStream_t s) {")
+    w("    return launch_eval_operands<L, %s>(use_float, lo, hi, n, stride, o, u, s);" % T_plain)
+    w("}")
     if L.numtype != "f32":
         w("static cudaError_t filter_f32(const LevelArgs& a, cudaStream_t s) { return launch_filter_f32<L>(a, s); }")
         w("static cudaError_t level_esc(int mode, const LevelArgs& a, unsigned blocks, cudaStream_t s) {")
@@ -620,8 +666,9 @@ def generate(lemma):
     w("extern const LemmaKernels kernels_%s;" % ns)
     prec = ("nullptr, nullptr, nullptr, nullptr, nullptr" if L.numtype == "f32" else
             "&{0}::filter_f32, &{0}::level_esc, &{0}::hoist_values, &{0}::prelude_f32, &{0}::filter_hoisted".format(ns))
-    w("const LemmaKernels kernels_%s = {\"%s\", 0x%016xull, %d, %d, %s, &%s::level, &%s::root_box, &%s::eval_batch, %s};" % (
+    w("const LemmaKernels kernels_%s = {\"%s\", 0x%016xull, %d, %d, %s, &%s::level, &%s::root_box, &%s::eval_batch, %s," % (
         ns, L.slug, L.fingerprint, L.nargs, len(L.bounds), "true" if L.numtype == "f32" else "false", ns, ns, ns, prec))
+    w("    &%s::eval_batch_plain, %d, &%s::eval_operands};" % (ns, len(operands), ns))
     w("")
     w("} // namespace sid")
     return ns, "\n".join(out) + "\n"

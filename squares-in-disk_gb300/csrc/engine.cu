@@ -17,6 +17,7 @@
 // engine; the server (sid_server_*) runs one lane per lemma on its own thread and stream and batches
 // the elements of all admitted requests of that lemma into each step.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstdarg>
@@ -76,6 +77,27 @@ void cuda_check(cudaError_t e, const char* what) {
     }
 }
 
+// Host-side fault injection (sid_debug_inject_failure): per kind, the number of failure points still to pass
+// before one fails (0: disarmed). Nothing is ever injected on the device.
+std::atomic<long long> g_inject_countdown[3];
+
+bool inject_now(int kind) {
+    std::atomic<long long>& c = g_inject_countdown[kind];
+    long long v = c.load();
+    while(v > 0) {
+        if(c.compare_exchange_weak(v, v - 1)) return v == 1;
+    }
+    return false;
+}
+
+/// Called before each launch of the proof and batch paths: an armed launch injection fails here, before
+/// anything is launched.
+void launch_gate(const char* what) {
+    if(inject_now(SID_INJECT_LAUNCH)) {
+        fail(SID_ERR_CUDA, "%s: %s (injected; nothing was launched)", what, cudaGetErrorString(cudaErrorLaunchFailure));
+    }
+}
+
 template<class F> int guarded(F&& f) {
     try {
         f();
@@ -111,13 +133,17 @@ template<class T> struct DevBuf {
     void reserve(std::size_t count) {
         if(count <= n) return;
         release();
-        cuda_check(cudaMalloc(&p, std::max<std::size_t>(count, 1) * sizeof(T)), "cudaMalloc");
+        cuda_check(inject_now(SID_INJECT_ALLOC) ? cudaErrorMemoryAllocation
+                                                : cudaMalloc(&p, std::max<std::size_t>(count, 1) * sizeof(T)),
+                   "cudaMalloc");
         n = count;
     }
     void reserve_on(std::size_t count, cudaStream_t s) {
         if(count <= n) return;
         release();
-        cuda_check(cudaMallocAsync(reinterpret_cast<void**>(&p), std::max<std::size_t>(count, 1) * sizeof(T), s),
+        cuda_check(inject_now(SID_INJECT_ALLOC)
+                       ? cudaErrorMemoryAllocation
+                       : cudaMallocAsync(reinterpret_cast<void**>(&p), std::max<std::size_t>(count, 1) * sizeof(T), s),
                    "cudaMallocAsync");
         n = count;
         ordered = s;
@@ -141,14 +167,16 @@ struct BoxList {
 
     void reserve(int na, std::uint64_t c, bool with_elem, bool with_path, bool with_depth, bool with_tag) {
         if(c <= cap && na == nargs) return;
-        nargs = na;
-        cap = c;
+        nargs = 0;   // the list has no capacity until every column is allocated (an allocation may fail)
+        cap = 0;
         box.release();
         box.reserve(std::size_t(na) * c);
         if(with_elem) { elem.release(); elem.reserve(c); }
         if(with_path) { path.release(); path.reserve(c); }
         if(with_depth) { depth.release(); depth.reserve(c); }
         if(with_tag) { tag.release(); tag.reserve(c); }
+        nargs = na;
+        cap = c;
     }
 };
 
@@ -214,6 +242,7 @@ struct Request {
     int state = SID_REQ_PENDING;
     bool admitted = false;
     std::string error;
+    int error_status = SID_OK;           // the status a failed request reports (SID_ERR_NOMEM, SID_ERR_CUDA, ...)
     Clock::time_point t_submit, t_admit, t_done;
     std::vector<double> criticals;
 };
@@ -238,17 +267,49 @@ struct HullArgs {
     const unsigned long long* hull_zhi;
     const std::uint8_t* depth;          // depth of each batch element
     const std::uint32_t* tag;           // request of each batch element
-    const ReqDev* req;
+    ReqDev* req;
     std::uint32_t n_elem;
     int nargs;
     // outputs: final (depth >= the request's generations) and non-final hulls
     double2* fin_box; std::uint8_t* fin_depth; std::uint32_t* fin_tag; unsigned long long* fin_count;
     double2* nf_box; std::uint8_t* nf_depth; std::uint32_t* nf_tag; unsigned long long* nf_count;
     std::uint64_t out_stride;
+    // node re-iteration (cpu_prover_core.hpp:113-134): with `iterate`, a hull that should_iterate accepts
+    // against its element's box (elem_box[v*elem_stride + e]) goes to the iteration list instead of being routed
+    bool iterate;
+    bool f32;                           // the lemma computes in float (the criteria then compare in float)
+    double single, volume;              // iteration_single_dimension / iteration_volume criteria
+    const double2* elem_box;
+    std::uint64_t elem_stride;
+    double2* it_box; std::uint8_t* it_depth; std::uint32_t* it_tag; unsigned long long* it_count;
+    std::uint64_t it_stride;            // variable stride of it_box (the iteration list's capacity)
 };
 
+/// CPUProverCore::p_should_iterate (cpu_prover_core.hpp:151-177) in the lemma's number type, with the
+/// reference's round-down arithmetic: re-run the static splits on the hull if some variable's hull width
+/// exceeds `single` times its old width (negated widths lb - ub, rounded down), or the hull's volume exceeds
+/// `volume` times the old volume (product of the negated first width and the other widths, rounded down).
+template<class T> __device__ bool should_iterate(const double2* nw, const double2* old, int nargs, T single, T volume) {
+    for(int i = 0; i < nargs; ++i) {
+        const T mnw = Dir<T>::sub_rd(T(nw[i].x), T(nw[i].y));
+        const T mow = Dir<T>::sub_rd(T(old[i].x), T(old[i].y));
+        if(Dir<T>::mul_rd(mow, single) > mnw) return true;
+    }
+    T mnv = Dir<T>::sub_rd(T(nw[0].x), T(nw[0].y));
+    T mov = Dir<T>::sub_rd(T(old[0].x), T(old[0].y));
+    for(int i = 1; i < nargs; ++i) {
+        mnv = Dir<T>::mul_rd(mnv, Dir<T>::sub_rd(T(nw[i].y), T(nw[i].x)));
+        mov = Dir<T>::mul_rd(mov, Dir<T>::sub_rd(T(old[i].y), T(old[i].x)));
+    }
+    return Dir<T>::mul_rd(mov, volume) > mnv;
+}
+
+constexpr int kMaxArgs = 32;   // variables of a lemma (the IR parser rejects more)
+
 /// Decode the per-element hull keys (AddToRange, cpu_prover_core.hpp:97-111: min of lower bounds, max
-/// of upper bounds, ties kept from the first leaf in static-split order) and route each non-empty hull.
+/// of upper bounds, ties kept from the first leaf in static-split order) and route each non-empty hull, or,
+/// with re-iteration, list it for another pass over the static splits (counted as a repeated node and a
+/// cuboid, cpu_prover_core.hpp:129-131).
 __global__ void k_hull_finalize(const HullArgs h) {
     const std::uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if(e >= h.n_elem) return;
@@ -256,32 +317,71 @@ __global__ void k_hull_finalize(const HullArgs h) {
     if(h.hull_lo[b0] == ~0ull) return;           // no leaf survived
     const std::uint8_t d = h.depth[e];
     const std::uint32_t t = h.tag[e];
-    const bool fin = d >= h.req[t].generations;
-    unsigned long long slot = atomicAdd(fin ? h.fin_count : h.nf_count, 1ull);
-    double2* out = fin ? h.fin_box : h.nf_box;
-    (fin ? h.fin_depth : h.nf_depth)[slot] = d;
-    (fin ? h.fin_tag : h.nf_tag)[slot] = t;
+    double2 box[kMaxArgs];
     for(int v = 0; v < h.nargs; ++v) {
         double lo = key_value(h.hull_lo[b0 + v]);
         double hi = key_value(h.hull_hi[b0 + v]);
         if(lo == 0.0) lo = (h.hull_zlo[b0 + v] & 1ull) ? -0.0 : 0.0;
         if(hi == 0.0) hi = (h.hull_zhi[b0 + v] & 1ull) ? -0.0 : 0.0;
-        out[std::uint64_t(v) * h.out_stride + slot] = make_double2(lo, hi);
+        box[v] = make_double2(lo, hi);
     }
+    if(h.iterate) {
+        double2 old[kMaxArgs];
+        for(int v = 0; v < h.nargs; ++v) old[v] = h.elem_box[std::uint64_t(v) * h.elem_stride + e];
+        const bool again = h.f32 ? should_iterate<float>(box, old, h.nargs, float(h.single), float(h.volume))
+                                 : should_iterate<double>(box, old, h.nargs, h.single, h.volume);
+        if(again) {
+            const unsigned long long slot = atomicAdd(h.it_count, 1ull);
+            h.it_depth[slot] = d;
+            h.it_tag[slot] = t;
+            for(int v = 0; v < h.nargs; ++v) h.it_box[std::uint64_t(v) * h.it_stride + slot] = box[v];
+            atomicAdd(&h.req[t].cnt[RC_REPEATED], 1ull);
+            atomicAdd(&h.req[t].cnt[RC_CUBOIDS], 1ull);
+            return;
+        }
+    }
+    const bool fin = d >= h.req[t].generations;
+    unsigned long long slot = atomicAdd(fin ? h.fin_count : h.nf_count, 1ull);
+    double2* out = fin ? h.fin_box : h.nf_box;
+    (fin ? h.fin_depth : h.nf_depth)[slot] = d;
+    (fin ? h.fin_tag : h.nf_tag)[slot] = t;
+    for(int v = 0; v < h.nargs; ++v) out[std::uint64_t(v) * h.out_stride + slot] = box[v];
 }
 
+/// Re-iteration of an element that is its own hull (a lemma without static splits): should_iterate compares
+/// the element with itself on every pass, so the element runs max_iter passes if it accepts, else one.
+struct RouteIteration {
+    int max_iter;
+    bool f32;
+    double single, volume;
+};
+
 /// Lemmas without static splits: every element is itself the only leaf of its static recursion
-/// (cpu_prover_core.hpp:250-256). Count it and route it by depth like k_hull_finalize.
+/// (cpu_prover_core.hpp:250-256). Count it (once per pass when re-iterated) and route it by depth like
+/// k_hull_finalize.
 __global__ void k_route_elements(const double2* box, std::uint64_t stride, const std::uint8_t* depth,
                                  const std::uint32_t* tag, std::uint64_t n, int nargs, ReqDev* req,
                                  double2* fin_box, std::uint8_t* fin_depth, std::uint32_t* fin_tag,
                                  unsigned long long* fin_count, double2* nf_box, std::uint8_t* nf_depth,
-                                 std::uint32_t* nf_tag, unsigned long long* nf_count, std::uint64_t out_stride) {
+                                 std::uint32_t* nf_tag, unsigned long long* nf_count, std::uint64_t out_stride,
+                                 const RouteIteration itr) {
     const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if(i >= n) return;
     const std::uint8_t d = depth[i];
     const std::uint32_t t = tag[i];
-    atomicAdd(&req[t].cnt[RC_LEAVES], 1ull);
+    unsigned long long passes = 1;
+    if(itr.max_iter > 1) {
+        double2 e[kMaxArgs];
+        for(int v = 0; v < nargs; ++v) e[v] = box[std::uint64_t(v) * stride + i];
+        const bool again = itr.f32 ? should_iterate<float>(e, e, nargs, float(itr.single), float(itr.volume))
+                                   : should_iterate<double>(e, e, nargs, itr.single, itr.volume);
+        if(again) passes = (unsigned long long)itr.max_iter;
+    }
+    atomicAdd(&req[t].cnt[RC_LEAVES], passes);
+    if(passes > 1) {
+        atomicAdd(&req[t].cnt[RC_REPEATED], passes - 1);
+        atomicAdd(&req[t].cnt[RC_CUBOIDS], passes - 1);
+    }
     const bool fin = d >= req[t].generations;
     const unsigned long long slot = atomicAdd(fin ? fin_count : nf_count, 1ull);
     double2* out = fin ? fin_box : nf_box;
@@ -445,13 +545,16 @@ struct Lane {
     std::uint32_t fp32_mask = ~0u;         // levels (dynamic d, static D + j) that use the float pass
     std::uint32_t noprop_mask = 0;         // float-pass levels without bound propagation (split-invariant form)
     std::uint32_t root_part_index = 0, root_part_count = 0;   // the root partition being admitted (sharding)
+    int max_iter = 1;                      // node re-iteration (max_iterations_per_node; <= 1: none)
+    double iter_single = 0.66, iter_volume = 0.25;
+    BoxList iter_in, iter_out;             // elements re-run on their hulls (re-iteration)
     std::uint64_t fanout = 1, root_fanout = 1;
     int sm_count = 1;
     int max_slots = kDefaultSlots;
     DevBuf<ReqDev> req_dev;
     std::vector<ReqDev> req_host;          // host copy of the table (counters as of the last read)
     std::vector<Request*> slot_req;
-    DevBuf<unsigned long long> counters;   // [0] out_count [1] fin [2] nf [3] escalation list length
+    DevBuf<unsigned long long> counters;   // [0] out_count [1] fin [2] nf [3] escalation list length [4] re-iterated
     DevBuf<unsigned int> overflow;
     DevBuf<unsigned long long> hull;       // 4 * step_cap * nargs
     BoxList step, fin, nonfin;
@@ -489,6 +592,17 @@ struct Lane {
     ~Lane() {
         if(st) cudaStreamSynchronize(st);
         if(own_stream && st) cudaStreamDestroy(st);
+    }
+
+    /// Node re-iteration settings (ProverSettings::max_iterations_per_node and the two criteria).
+    void set_iteration(int max_iterations, float volume, float single) {
+        max_iter = max_iterations;
+        iter_volume = double(volume);
+        iter_single = double(single);
+        if(max_iter > 1) {
+            iter_in.reserve(n, std::max(iter_in.cap, step_cap), false, false, true, true);
+            iter_out.reserve(n, std::max(iter_out.cap, step_cap), false, false, true, true);
+        }
     }
 
     void configure(std::uint64_t step_elements, bool fp32, std::uint32_t mask = ~0u, std::uint32_t noprop = 0) {
@@ -701,6 +815,7 @@ struct Lane {
     void launch(int mode, const LevelArgs& a0, int level) {
         const std::uint64_t total = a0.n_in * std::uint64_t(a0.nsub);
         if(total == 0) return;
+        launch_gate("level kernel launch");
         // the root's first split of a sharded proof runs the dense kernel, which applies the part filter
         const bool level_fp32 = fp32_first && level < SID_MAX_LEVELS && ((fp32_mask >> level) & 1u) && a0.part_count <= 1;
         if(level_fp32) level_children[std::size_t(level)] += total;
@@ -919,6 +1034,7 @@ struct Lane {
         gather.reserve(gather_host.size());
         cuda_check(cudaMemcpyAsync(gather.p, gather_host.data(), gather_host.size() * sizeof(GatherEntry),
                                    cudaMemcpyHostToDevice, st), "gather table");
+        launch_gate("gather");
         k_gather<<<unsigned((B + 127) / 128), 128, 0, st>>>(gather.p, int(gather_host.size()), B, req_dev.p, n, step.box.p,
                                                             step.cap, step.depth.p, step.tag.p);
         cuda_check(cudaGetLastError(), "gather");
@@ -926,32 +1042,57 @@ struct Lane {
         set_counter(counters.p + 1, 0);
         set_counter(counters.p + 2, 0);
         if(stat.empty()) {
+            const RouteIteration itr{max_iter, lem->k->is_f32, iter_single, iter_volume};
             k_route_elements<<<unsigned((B + 127) / 128), 128, 0, st>>>(
                 step.box.p, step.cap, step.depth.p, step.tag.p, B, n, req_dev.p, fin.box.p, fin.depth.p, fin.tag.p,
-                counters.p + 1, nonfin.box.p, nonfin.depth.p, nonfin.tag.p, counters.p + 2, step_cap);
+                counters.p + 1, nonfin.box.p, nonfin.depth.p, nonfin.tag.p, counters.p + 2, step_cap, itr);
             cuda_check(cudaGetLastError(), "route elements");
         } else {
-            // reset hulls: lo keys to max, hi keys to 0, first-zero paths to max
-            cuda_check(cudaMemsetAsync(hull.p, 0xff, B * n * sizeof(unsigned long long), st), "hull reset");
-            cuda_check(cudaMemsetAsync(hull.p + step_cap * n, 0, B * n * sizeof(unsigned long long), st), "hull reset");
-            cuda_check(cudaMemsetAsync(hull.p + 2 * step_cap * n, 0xff, 2 * step_cap * n * sizeof(unsigned long long), st),
-                       "hull reset");
-            run_static(0, step.box.p, step.cap, nullptr, nullptr, step.tag.p, 0, B, MODE_HULL);
-            HullArgs h{};
-            h.hull_lo = hull.p;
-            h.hull_hi = hull.p + step_cap * n;
-            h.hull_zlo = hull.p + 2 * step_cap * n;
-            h.hull_zhi = hull.p + 3 * step_cap * n;
-            h.depth = step.depth.p;
-            h.tag = step.tag.p;
-            h.req = req_dev.p;
-            h.n_elem = std::uint32_t(B);
-            h.nargs = n;
-            h.fin_box = fin.box.p; h.fin_depth = fin.depth.p; h.fin_tag = fin.tag.p; h.fin_count = counters.p + 1;
-            h.nf_box = nonfin.box.p; h.nf_depth = nonfin.depth.p; h.nf_tag = nonfin.tag.p; h.nf_count = counters.p + 2;
-            h.out_stride = step_cap;
-            k_hull_finalize<<<unsigned((B + 127) / 128), 128, 0, st>>>(h);
-            cuda_check(cudaGetLastError(), "hull finalize");
+            // pass p over the static splits (p = 1, 2, ...): hulls of the elements, then routing; with re-iteration
+            // (p < max_iter) a hull that should_iterate accepts is re-run as the element of the next pass
+            // (p_handle_cuboid_nf, cpu_prover_core.hpp:113-134)
+            const BoxList* in = &step;
+            std::uint64_t n_elem = B;
+            for(int pass = 1; n_elem > 0; ++pass) {
+                // reset hulls: lo keys to max, hi keys to 0, first-zero paths to max
+                cuda_check(cudaMemsetAsync(hull.p, 0xff, n_elem * n * sizeof(unsigned long long), st), "hull reset");
+                cuda_check(cudaMemsetAsync(hull.p + step_cap * n, 0, n_elem * n * sizeof(unsigned long long), st),
+                           "hull reset");
+                cuda_check(cudaMemsetAsync(hull.p + 2 * step_cap * n, 0xff, 2 * step_cap * n * sizeof(unsigned long long),
+                                           st), "hull reset");
+                run_static(0, in->box.p, in->cap, nullptr, nullptr, in->tag.p, 0, n_elem, MODE_HULL);
+                HullArgs h{};
+                h.hull_lo = hull.p;
+                h.hull_hi = hull.p + step_cap * n;
+                h.hull_zlo = hull.p + 2 * step_cap * n;
+                h.hull_zhi = hull.p + 3 * step_cap * n;
+                h.depth = in->depth.p;
+                h.tag = in->tag.p;
+                h.req = req_dev.p;
+                h.n_elem = std::uint32_t(n_elem);
+                h.nargs = n;
+                h.fin_box = fin.box.p; h.fin_depth = fin.depth.p; h.fin_tag = fin.tag.p; h.fin_count = counters.p + 1;
+                h.nf_box = nonfin.box.p; h.nf_depth = nonfin.depth.p; h.nf_tag = nonfin.tag.p; h.nf_count = counters.p + 2;
+                h.out_stride = step_cap;
+                h.iterate = pass < max_iter;
+                if(h.iterate) {
+                    h.f32 = lem->k->is_f32;
+                    h.single = iter_single;
+                    h.volume = iter_volume;
+                    h.elem_box = in->box.p;
+                    h.elem_stride = in->cap;
+                    BoxList& out = (in == &iter_in) ? iter_out : iter_in;
+                    h.it_box = out.box.p; h.it_depth = out.depth.p; h.it_tag = out.tag.p; h.it_count = counters.p + 4;
+                    h.it_stride = out.cap;
+                    set_counter(counters.p + 4, 0);
+                }
+                launch_gate("hull finalize");
+                k_hull_finalize<<<unsigned((n_elem + 127) / 128), 128, 0, st>>>(h);
+                cuda_check(cudaGetLastError(), "hull finalize");
+                if(!h.iterate) break;
+                n_elem = read_counter(counters.p + 4);
+                in = (in == &iter_in) ? &iter_out : &iter_in;
+            }
         }
         const std::uint64_t nfin = read_counter(counters.p + 1);
         const std::uint64_t nnf = read_counter(counters.p + 2);
@@ -1049,12 +1190,13 @@ void poll_batch_sample(Lemma* lem) {
 /// saves the sort when the float test decides nearly every cuboid. Every call whose predecessor's sample has
 /// arrived counts the cuboids that needed the double constraints.
 void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const double* hi, std::uint64_t n, double* out_lo,
-                        double* out_hi, std::int8_t* verdict, cudaStream_t s, std::uint64_t stride = 0) {
+                        double* out_hi, std::int8_t* verdict, cudaStream_t s, std::uint64_t stride = 0, bool plain = false) {
     if(stride == 0) stride = n;
     const int nargs = lem->ir.nargs;
     profile_mark(eng, s);
     poll_batch_sample(lem);
-    const bool want_order = lem->batch_order == SID_BATCH_ORDER_ON ||
+    // the all-double kernel (plain) always orders: nearly every cuboid there reaches the double constraints
+    const bool want_order = plain || lem->batch_order == SID_BATCH_ORDER_ON ||
                             (lem->batch_order == SID_BATCH_ORDER_AUTO &&
                              (lem->batch_double_share < 0.0 || lem->batch_double_share > kOrderShare));
     const std::uint32_t* order = nullptr;
@@ -1086,7 +1228,16 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
         if(eng->batch_profile) eng->batch_launches += 5;
     }
     profile_mark(eng, s);
-    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order, stride, nullptr, nullptr, nullptr};
+    BatchArgs a{lo, hi, out_lo, out_hi, verdict, n, order, stride, nullptr, nullptr, nullptr, 0u};
+    a.slow_blocks = unsigned(std::max(eng->sm_count, 1)) * 8u;
+    launch_gate("eval batch");
+    if(plain) {
+        cuda_check(lem->k->eval_batch_plain(a, s), "eval batch (plain)");
+        if(eng->batch_profile) eng->batch_launches += n > 0 ? 1u : 0u;
+        profile_mark(eng, s);
+        profile_mark(eng, s);
+        return;
+    }
     const bool defers = batch_defers(nargs);
     if(defers) {
         eng->batch_slow.reserve(std::size_t(n));
@@ -1096,12 +1247,16 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
     }
     const bool sample = !lem->batch_sample_pending && !lem->k->is_f32 && n > 0;
     if(sample) {
-        if(!lem->batch_sample_host) {   // once per lemma: pinned (device-visible) host word, cleared counter
-            cuda_check(cudaMallocHost(reinterpret_cast<void**>(&lem->batch_sample_host), sizeof(unsigned long long)),
-                       "batch sample");
-            cuda_check(cudaEventCreateWithFlags(&lem->batch_sample_ev, cudaEventDisableTiming), "batch sample");
+        if(!lem->batch_sample.p) {   // once per lemma: cleared device counter, pinned (device-visible) host word
             lem->batch_sample.reserve(1);
             cuda_check(cudaMemsetAsync(lem->batch_sample.p, 0, sizeof(unsigned long long), s), "batch sample");
+        }
+        if(!lem->batch_sample_ev) {
+            cuda_check(cudaEventCreateWithFlags(&lem->batch_sample_ev, cudaEventDisableTiming), "batch sample");
+        }
+        if(!lem->batch_sample_host) {
+            cuda_check(cudaMallocHost(reinterpret_cast<void**>(&lem->batch_sample_host), sizeof(unsigned long long)),
+                       "batch sample");
         }
         a.double_rows = lem->batch_sample.p;
     }
@@ -1127,7 +1282,7 @@ void check_precision(int precision) {
     }
 }
 
-constexpr char kCheckpointMagic[8] = {'S', 'I', 'D', 'C', 'K', 'P', 'T', '1'};
+constexpr char kCheckpointMagic[8] = {'S', 'I', 'D', 'C', 'K', 'P', 'T', '2'};   // 2: repeated-node counter
 
 void write_checkpoint(const char* path, const ProofState& ps) {
     std::string tmp = std::string(path) + ".part";
@@ -1180,9 +1335,6 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
                const std::uint32_t* mask_override = nullptr, const ProofState* resume = nullptr,
                const std::uint32_t* noprop_override = nullptr) {
     Lemma* lem = get_lemma(eng, lemma_id);
-    if(o.max_iterations_per_node > 1) {
-        fail(SID_ERR_UNSUPPORTED, "max_iterations_per_node > 1 (re-iteration of a node) is not supported; use 1");
-    }
     auto& slot = eng->prove_lanes[lemma_id];
     if(!slot) slot.reset(new Lane(eng, lem, eng->stream, false, eng->sm_count, 1));
     Lane& lane = *slot;
@@ -1192,6 +1344,7 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
     lane.configure(step_override ? step_override : step, o.precision != SID_PRECISION_PLAIN,
                    mask_override ? *mask_override : (tuned ? lem->tuning.fp32_level_mask : o.fp32_level_mask),
                    noprop_override ? *noprop_override : (tuned ? lem->tuning.fp32_noprop_mask : o.fp32_noprop_mask));
+    lane.set_iteration(o.max_iterations_per_node, o.iteration_volume_criterion, o.iteration_single_dimension_criterion);
 
     if(o.part_count > 1 && o.part_index >= o.part_count) {
         fail(SID_ERR_INVALID, "part_index %u outside part_count %u", o.part_index, o.part_count);
@@ -1286,7 +1439,7 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
     res->num_cuboids = last.cnt[RC_CUBOIDS];
     res->num_leaf_cuboids = last.cnt[RC_LEAVES];
     res->num_critical_cuboids = last.cnt[RC_CRITICALS];
-    res->num_repeated_nodes = 0;
+    res->num_repeated_nodes = last.cnt[RC_REPEATED];
     res->criticals_stored = std::min<std::uint64_t>(res->num_critical_cuboids, r.crit_cap);
     res->escalated = last.cnt[RC_ESCALATED];
     res->seconds = double(ms) / 1000.0;
@@ -1320,86 +1473,135 @@ struct sid_server {
 
     std::uint64_t budget() const { return opts.memory_budget_bytes ? opts.memory_budget_bytes : (std::uint64_t(16) << 30); }
 
-    void fail_all(Worker& w, const std::string& msg) {
+    /// The lane of a worker: its own stream, the lemma's kernels and scratch, configured for the server.
+    void make_lane(Worker* w) {
+        cuda_check(cudaSetDevice(eng->device), "cudaSetDevice");
+        Lemma* lem = eng->lemmas[std::size_t(w->lemma_id)].get();
+        cudaStream_t s = nullptr;
+        cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+        const int slots = int(opts.max_requests_per_lane > 0 ? opts.max_requests_per_lane : kDefaultSlots);
+        std::unique_ptr<sid::Lane> lane;
+        try {
+            lane.reset(new Lane(eng, lem, s, true, eng->sm_count, slots));
+        } catch(...) {
+            cudaStreamDestroy(s);
+            throw;
+        }
+        const bool tuned = opts.precision == SID_PRECISION_FP32_TUNED && lem->tuned;
+        lane->configure(opts.step_elements > 0 ? std::uint64_t(opts.step_elements)
+                                               : (tuned ? std::uint64_t(lem->tuning.step_elements) : kDefaultStep),
+                        opts.precision != SID_PRECISION_PLAIN, tuned ? lem->tuning.fp32_level_mask : ~0u,
+                        tuned ? lem->tuning.fp32_noprop_mask : ~0u);
+        lane->set_iteration(opts.max_iterations_per_node, opts.iteration_volume_criterion,
+                            opts.iteration_single_dimension_criterion);
+        w->lane = std::move(lane);
+    }
+
+    /// One round of a worker: admit what fits, run one step over the admitted requests, retire the finished ones.
+    void serve_round(Worker* w, std::vector<Request*>& held) {
+        Lane& lane = *w->lane;
+        std::vector<Request*> admit;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            std::vector<std::uint64_t> need;
+            for(Request* r : w->pending) need.push_back(lane.initial_bytes(*r));
+            const std::size_t k = plan::admit_count(need, mem_used, budget(), w->active.size(),
+                                                    std::size_t(lane.free_slots()));
+            for(std::size_t i = 0; i < k; ++i) {
+                Request* r = w->pending.front();
+                w->pending.pop_front();
+                r->bytes = need[i];          // charged to the budget from here on, whatever happens next
+                mem_used += need[i];
+                admit.push_back(r);
+                held.push_back(r);
+            }
+        }
+        for(Request* r : admit) {
+            lane.admit(r);
+            std::lock_guard<std::mutex> lk(mu);
+            r->state = SID_REQ_RUNNING;
+            r->admitted = true;
+            r->t_admit = Clock::now();
+            r->view = lane.counters_of(r);
+            w->active.push_back(r);
+        }
+        if(!w->active.empty()) lane.run_step(w->active);
+        std::vector<Request*> done;
+        for(Request* r : w->active) if(lane.queue_size(r) == 0) done.push_back(r);
+        std::vector<sid::ReqDev> final_counts;
+        for(Request* r : done) {
+            lane.fetch_criticals(r);
+            final_counts.push_back(lane.counters_of(r));
+            lane.release(r);
+            held.erase(std::find(held.begin(), held.end(), r));
+        }
         std::lock_guard<std::mutex> lk(mu);
-        for(Request* r : w.active) { r->state = SID_REQ_FAILED; r->error = msg; r->t_done = Clock::now(); }
-        for(Request* r : w.pending) { r->state = SID_REQ_FAILED; r->error = msg; r->t_done = Clock::now(); }
-        w.active.clear();
-        w.pending.clear();
+        mem_used += std::uint64_t(std::max<long long>(0, lane.take_grown_bytes()));
+        for(Request* r : w->active) if(r->slot >= 0) r->view = lane.counters_of(r);
+        for(std::size_t i = 0; i < done.size(); ++i) {
+            Request* r = done[i];
+            r->view = final_counts[i];
+            mem_used -= std::min(mem_used, r->bytes);
+            r->state = SID_REQ_DONE;
+            r->t_done = Clock::now();
+            w->active.erase(std::find(w->active.begin(), w->active.end(), r));
+        }
+        if(!done.empty()) cv_done.notify_all();
+    }
+
+    /// After a round threw: the requests admitted to the lane fail (their device state is dropped and their
+    /// memory returned to the budget); the lane and the waiting requests carry on. Without a lane (its set-up
+    /// failed) no request can run, so the waiting ones fail too.
+    void recover(Worker* w, std::vector<Request*>& held, int status, const std::string& msg) {
+        if(w->lane) {
+            for(Request* r : held) {
+                try { w->lane->release(r); } catch(...) {}
+            }
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        const auto now = Clock::now();
+        for(Request* r : held) {
+            r->state = SID_REQ_FAILED;
+            r->error = msg;
+            r->error_status = status;
+            r->t_done = now;
+            mem_used -= std::min(mem_used, r->bytes);
+        }
+        held.clear();
+        w->active.clear();
+        if(!w->lane) {
+            for(Request* r : w->pending) {
+                r->state = SID_REQ_FAILED;
+                r->error = msg;
+                r->error_status = status;
+                r->t_done = now;
+            }
+            w->pending.clear();
+        }
         cv_done.notify_all();
     }
 
     void worker_loop(Worker* w) {
         std::vector<Request*> held;   // admitted requests whose device state must be released on exit
-        try {
-            cuda_check(cudaSetDevice(eng->device), "cudaSetDevice");
-            cudaStream_t s = nullptr;
-            cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
-            Lemma* lem = eng->lemmas[std::size_t(w->lemma_id)].get();
-            const int slots = int(opts.max_requests_per_lane > 0 ? opts.max_requests_per_lane : kDefaultSlots);
-            w->lane.reset(new Lane(eng, lem, s, true, eng->sm_count, slots));
-            const bool tuned = opts.precision == SID_PRECISION_FP32_TUNED && lem->tuned;
-            w->lane->configure(opts.step_elements > 0 ? std::uint64_t(opts.step_elements)
-                                                      : (tuned ? std::uint64_t(lem->tuning.step_elements) : kDefaultStep),
-                               opts.precision != SID_PRECISION_PLAIN, tuned ? lem->tuning.fp32_level_mask : ~0u,
-                               tuned ? lem->tuning.fp32_noprop_mask : ~0u);
-            Lane& lane = *w->lane;
-            for(;;) {
-                std::vector<Request*> admit;
-                {
-                    std::unique_lock<std::mutex> lk(mu);
-                    w->cv.wait(lk, [&] { return stopping || !w->pending.empty() || !w->active.empty(); });
-                    if(stopping) break;
-                    std::vector<std::uint64_t> need;
-                    for(Request* r : w->pending) need.push_back(lane.initial_bytes(*r));
-                    const std::size_t k = plan::admit_count(need, mem_used, budget(), w->active.size(),
-                                                            std::size_t(lane.free_slots()));
-                    for(std::size_t i = 0; i < k; ++i) {
-                        admit.push_back(w->pending.front());
-                        w->pending.pop_front();
-                        mem_used += need[i];
-                    }
-                }
-                for(Request* r : admit) {
-                    held.push_back(r);
-                    lane.admit(r);
-                    std::lock_guard<std::mutex> lk(mu);
-                    r->state = SID_REQ_RUNNING;
-                    r->admitted = true;
-                    r->t_admit = Clock::now();
-                    r->view = lane.counters_of(r);
-                    w->active.push_back(r);
-                }
-                if(!w->active.empty()) lane.run_step(w->active);
-                std::vector<Request*> done;
-                for(Request* r : w->active) if(lane.queue_size(r) == 0) done.push_back(r);
-                std::vector<sid::ReqDev> final_counts;
-                for(Request* r : done) {
-                    lane.fetch_criticals(r);
-                    final_counts.push_back(lane.counters_of(r));
-                    lane.release(r);
-                    held.erase(std::find(held.begin(), held.end(), r));
-                }
-                std::lock_guard<std::mutex> lk(mu);
-                mem_used += std::uint64_t(std::max<long long>(0, lane.take_grown_bytes()));
-                for(Request* r : w->active) if(r->slot >= 0) r->view = lane.counters_of(r);
-                for(std::size_t i = 0; i < done.size(); ++i) {
-                    Request* r = done[i];
-                    r->view = final_counts[i];
-                    mem_used -= std::min(mem_used, r->bytes);
-                    r->state = SID_REQ_DONE;
-                    r->t_done = Clock::now();
-                    w->active.erase(std::find(w->active.begin(), w->active.end(), r));
-                }
-                if(!done.empty()) cv_done.notify_all();
+        for(;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                w->cv.wait(lk, [&] { return stopping || !w->pending.empty() || !w->active.empty(); });
+                if(stopping) break;
             }
-        } catch(const SidError& e) {
-            fail_all(*w, e.msg);
-        } catch(const std::exception& e) {
-            fail_all(*w, e.what());
+            try {
+                if(!w->lane) make_lane(w);
+                serve_round(w, held);
+            } catch(const SidError& e) {
+                recover(w, held, e.status, e.msg);
+            } catch(const std::exception& e) {
+                recover(w, held, SID_ERR_INVALID, e.what());
+            }
         }
         if(w->lane) {
-            for(Request* r : held) w->lane->release(r);
+            for(Request* r : held) {
+                try { w->lane->release(r); } catch(...) {}
+            }
             w->lane.reset();
         }
     }
@@ -1411,6 +1613,7 @@ struct sid_server {
         st->num_leaf_cuboids = r.view.cnt[RC_LEAVES];
         st->num_critical_cuboids = r.view.cnt[RC_CRITICALS];
         st->escalated = r.view.cnt[RC_ESCALATED];
+        st->num_repeated_nodes = r.view.cnt[RC_REPEATED];
         st->criticals_stored = std::min<std::uint64_t>(r.view.cnt[RC_CRITICALS], r.crit_cap);
         st->proved = r.state == SID_REQ_DONE && r.view.cnt[RC_CRITICALS] == 0;
         if(r.admitted) st->seconds_queued = std::chrono::duration<double>(r.t_admit - r.t_submit).count();
@@ -1607,6 +1810,38 @@ int sid_eval_batch_device(sid_engine* engine, int lemma_id, const double* lo, co
     });
 }
 
+int sid_eval_batch_plain_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
+                                double* out_lo, double* out_hi, int8_t* verdict, void* stream) {
+    return guarded([&] {
+        Lemma* l = get_lemma(engine, lemma_id);
+        if(l->k->is_f32) fail(SID_ERR_UNSUPPORTED, "batch evaluation supports double lemmas");
+        if(n > 0 && (!lo || !hi || !out_lo || !out_hi || !verdict)) fail(SID_ERR_INVALID, "null buffer");
+        set_device(engine);
+        eval_batch_ordered(engine, l, lo, hi, n, out_lo, out_hi, verdict, static_cast<cudaStream_t>(stream), 0, true);
+    });
+}
+
+int sid_lemma_operands(sid_engine* engine, int lemma_id, uint32_t* count) {
+    return guarded([&] {
+        Lemma* l = get_lemma(engine, lemma_id);
+        if(!count) fail(SID_ERR_INVALID, "null output");
+        *count = std::uint32_t(l->k->n_operands);
+    });
+}
+
+int sid_eval_operands_device(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
+                             int use_float, double* out_lohi, int8_t* out_undefined, void* stream) {
+    return guarded([&] {
+        Lemma* l = get_lemma(engine, lemma_id);
+        if(n == 0 || l->k->n_operands == 0) return;
+        if(!lo || !hi || !out_lohi || !out_undefined) fail(SID_ERR_INVALID, "null buffer");
+        set_device(engine);
+        cuda_check(l->k->eval_operands(use_float ? 1 : 0, lo, hi, n, 0, reinterpret_cast<double2*>(out_lohi), out_undefined,
+                                       static_cast<cudaStream_t>(stream)),
+                   "operand kernel");
+    });
+}
+
 int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const double* hi, uint64_t n,
                    double* out_lo, double* out_hi, int8_t* verdict) {
     return guarded([&] {
@@ -1680,6 +1915,14 @@ int sid_eval_batch(sid_engine* engine, int lemma_id, const double* lo, const dou
             throw;
         }
         for(cudaEvent_t e : evs) cudaEventDestroy(e);
+    });
+}
+
+int sid_debug_inject_failure(int kind, int64_t countdown) {
+    return guarded([&] {
+        if(kind != SID_INJECT_ALLOC && kind != SID_INJECT_LAUNCH) fail(SID_ERR_INVALID, "unknown injection kind %d", kind);
+        if(countdown < 0) fail(SID_ERR_INVALID, "negative countdown");
+        g_inject_countdown[kind].store((long long)countdown);
     });
 }
 
@@ -1836,6 +2079,9 @@ void sid_server_opts_default(sid_server_opts* o) {
     o->generation_count = 8;
     o->max_criticals_per_request = 1024;
     o->max_requests_per_lane = kDefaultSlots;
+    o->max_iterations_per_node = 1;
+    o->iteration_volume_criterion = 0.25f;
+    o->iteration_single_dimension_criterion = 0.66f;
 }
 
 int sid_server_create(sid_engine* engine, const sid_server_opts* opts, sid_server** out) {
@@ -1911,7 +2157,9 @@ int sid_request_poll(sid_server* server, uint64_t request_id, sid_request_status
         auto it = server->reqs.find(request_id);
         if(it == server->reqs.end()) fail(SID_ERR_INVALID, "unknown request %llu", (unsigned long long)request_id);
         sid_server::fill_status(*it->second, status);
-        if(it->second->state == SID_REQ_FAILED) fail(SID_ERR_CUDA, "request failed: %s", it->second->error.c_str());
+        if(it->second->state == SID_REQ_FAILED) {
+            fail(it->second->error_status, "request failed: %s", it->second->error.c_str());
+        }
     });
 }
 
@@ -1926,7 +2174,7 @@ int sid_request_wait(sid_server* server, uint64_t request_id, int timeout_ms, si
         if(timeout_ms < 0) server->cv_done.wait(lk, finished);
         else server->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished);
         sid_server::fill_status(*r, status);
-        if(r->state == SID_REQ_FAILED) fail(SID_ERR_CUDA, "request failed: %s", r->error.c_str());
+        if(r->state == SID_REQ_FAILED) fail(r->error_status, "request failed: %s", r->error.c_str());
         if(!finished()) fail(SID_ERR_TIMEOUT, "request %llu not finished after %d ms", (unsigned long long)request_id,
                              timeout_ms);
     });

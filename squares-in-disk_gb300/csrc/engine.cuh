@@ -30,7 +30,8 @@ enum ReqCounter : int {
     RC_ESCALATED = 3,    // precision form: children evaluated in double
     RC_QSIZE = 4,        // elements in the request's queue (appended with atomics)
     RC_OVERFLOW = 5,     // a queue append did not fit (the host sizes queues so that this stays 0)
-    RC_N = 6
+    RC_REPEATED = 6,     // nodes re-iterated on their hull (max_iterations_per_node > 1)
+    RC_N = 7
 };
 
 /// Device state of one request (a proof, or a set of sub-boxes of a lemma): counters, its frontier queue
@@ -798,6 +799,7 @@ struct BatchArgs {
     // evaluates them on full warps; slow holds up to n cuboid indices, *slow_count is cleared per launch
     std::uint64_t* slow;
     unsigned long long* slow_count;
+    unsigned slow_blocks;         // grid of k_eval_batch_slow: the device's SMs x 8 resident blocks (0: 1216)
 };
 
 /// Whether the batch kernel of a lemma with `nargs` variables defers its rare expensive work (the bounds in
@@ -1062,6 +1064,52 @@ template<class L, class T> __global__ void __launch_bounds__(128, 8) k_eval_batc
     }
 }
 
+/// The all-double form of the batch evaluation, in the reference's order (the innermost leaf step of
+/// cpu_prover_core.hpp:221-256): propagate after a change of the last variable (it_limit = nargs,
+/// rec_limit = 4), then the constraints of the last row in the lemma's own type, stopping at the first
+/// violated one. No float test, no stages and no deferred list: the FP64 baseline of k_eval_batch, whose
+/// outputs it equals bit for bit (a float refutation is a double refutation). One cuboid per thread,
+/// through `order` when given.
+template<class L, class T> __global__ void __launch_bounds__(128, 8) k_eval_batch_plain(const BatchArgs a) {
+    constexpr int N = L::NARGS;
+    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(t >= a.n) return;
+    const std::uint64_t st = a.stride ? a.stride : a.n;
+    const std::uint64_t i = a.order ? std::uint64_t(a.order[t]) : t;
+    Iv<T> box[N];
+    #pragma unroll
+    for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
+    std::int8_t vd = 0;
+    if(propagate<L, T>(N - 1, box, N, 4)) vd = 1;
+    else if(!L::template rows_ok<T>(N - 1, N, box)) vd = 2;
+    a.verdict[i] = vd;
+    #pragma unroll
+    for(int v = 0; v < N; ++v) {
+        a.out_lo[std::uint64_t(v) * st + i] = double(box[v].lo);
+        a.out_hi[std::uint64_t(v) * st + i] = double(box[v].hi);
+    }
+}
+
+/// Endpoint dump: every expression the lemma's constraints compare (L::operands, in the oracle's order) on
+/// each of n boxes, in T: the box as given (double), or rounded outward to float (the precision form's float
+/// pass). Boxes lo[v*stride + i], hi[v*stride + i]; operand j of box i goes to out[j*stride + i] (lo, hi) and
+/// und[j*stride + i] (1 if possibly undefined).
+template<class L, class T> __global__ void __launch_bounds__(128) k_eval_operands(const double* lo, const double* hi,
+                                                                                   std::uint64_t n, std::uint64_t stride,
+                                                                                   double2* out, std::int8_t* und) {
+    constexpr int N = L::NARGS;
+    const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    Iv<T> box[N];
+    #pragma unroll
+    for(int v = 0; v < N; ++v) {
+        const double l = lo[std::uint64_t(v) * stride + i], h = hi[std::uint64_t(v) * stride + i];
+        if constexpr(sizeof(T) == sizeof(double)) box[v] = {T(l), T(h), false};
+        else box[v] = {__double2float_rd(l), __double2float_ru(h), false};
+    }
+    L::template operands<T>(box, out, und, stride, i);
+}
+
 /// Host-side launch table of one compiled lemma.
 struct LemmaKernels {
     const char* slug;
@@ -1081,6 +1129,10 @@ struct LemmaKernels {
     cudaError_t (*prelude_f32)(int level, const LevelArgs& a, std::uint64_t n_items, float2* hval, std::uint64_t* hbits,
                                cudaStream_t s);
     cudaError_t (*filter_hoisted)(int level, const LevelArgs& a, cudaStream_t s);
+    cudaError_t (*eval_batch_plain)(const BatchArgs& a, cudaStream_t s);
+    int n_operands;                   // expressions compared by the constraints (L::NOPERANDS)
+    cudaError_t (*eval_operands)(int use_float, const double* lo, const double* hi, std::uint64_t n, std::uint64_t stride,
+                                 double2* out, std::int8_t* und, cudaStream_t s);
 };
 
 template<class L, class T> cudaError_t launch_level(int mode, const LevelArgs& a, cudaStream_t s) {
@@ -1155,12 +1207,33 @@ template<class L, class T> cudaError_t launch_eval_batch(const BatchArgs& a, cud
             // grid-stride over the deferred list, whose length only the device knows: enough blocks to fill
             // the GPU
             const std::uint64_t want_blocks = (a.n + threads - 1) / threads;
-            const std::uint64_t slow_blocks = want_blocks < 152u * 8u ? want_blocks : 152u * 8u;
+            const std::uint64_t fill = a.slow_blocks ? a.slow_blocks : 1216u;
+            const std::uint64_t slow_blocks = want_blocks < fill ? want_blocks : fill;
             k_eval_batch_slow<L, T><<<unsigned(slow_blocks), threads, 0, s>>>(a);
             return cudaGetLastError();
         }
     }
     k_eval_batch<L, T, false><<<unsigned(blocks), threads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template<class L, class T> cudaError_t launch_eval_batch_plain(const BatchArgs& a, cudaStream_t s) {
+    if(a.n == 0) return cudaSuccess;
+    const std::uint64_t blocks = (a.n + 127) / 128;
+    if(blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    k_eval_batch_plain<L, T><<<unsigned(blocks), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template<class L, class T> cudaError_t launch_eval_operands(int use_float, const double* lo, const double* hi, std::uint64_t n,
+                                                            std::uint64_t stride, double2* out, std::int8_t* und,
+                                                            cudaStream_t s) {
+    if(n == 0 || L::NOPERANDS == 0) return cudaSuccess;
+    if(stride == 0) stride = n;
+    const std::uint64_t blocks = (n + 127) / 128;
+    if(blocks > 0x7fffffffull || stride < n) return cudaErrorInvalidValue;
+    if(use_float) k_eval_operands<L, float><<<unsigned(blocks), 128, 0, s>>>(lo, hi, n, stride, out, und);
+    else k_eval_operands<L, T><<<unsigned(blocks), 128, 0, s>>>(lo, hi, n, stride, out, und);
     return cudaGetLastError();
 }
 

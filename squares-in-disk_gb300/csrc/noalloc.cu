@@ -22,7 +22,7 @@ using namespace sid;
 // 8 MiB per device, held from library load until process exit.
 constexpr std::size_t kScratchBytes = std::size_t(8) << 20;
 constexpr std::size_t kScratchWords = kScratchBytes / sizeof(unsigned long long);
-// header: words 0..11 the request record the level kernel counts into (ReqDev: word 1 = leaves),
+// header: words 0..12 the request record the level kernel counts into (ReqDev: word 1 = leaves),
 // word 16 the list-overflow flag; keys start at word 32
 constexpr std::size_t kHeaderWords = 32;
 static_assert(sizeof(ReqDev) <= 16 * sizeof(unsigned long long), "request record must fit the header");
@@ -83,7 +83,18 @@ extern "C" int sid_leaf_hull_noalloc(sid_engine* engine, int lemma_id, const dou
     if(view.last_static_arg < 0) {
         return fail_status(SID_ERR_UNSUPPORTED, "sid_leaf_hull_noalloc: the lemma has no static split");
     }
-    if(n == 0) return SID_OK;
+    if(view.kernels->is_f32) {
+        return fail_status(SID_ERR_UNSUPPORTED, "sid_leaf_hull_noalloc: supports double lemmas (as sid_eval_batch)");
+    }
+    if(view.device < 0 || view.device >= kMaxDevices) return fail_status(SID_ERR_INVALID, "device id out of range");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if(n == 0) {
+        // no parents: no leaves
+        if(!leaves) return SID_OK;
+        cudaError_t e = cudaSetDevice(view.device);
+        if(e == cudaSuccess) e = cudaMemsetAsync(leaves, 0, sizeof(unsigned long long), s);
+        return e == cudaSuccess ? SID_OK : cuda_status(e, "cudaMemsetAsync(leaves)");
+    }
     if(!boxes || !hulls || !nonempty) return fail_status(SID_ERR_INVALID, "sid_leaf_hull_noalloc: null buffer");
     if(n > kMaxItemVars / std::uint64_t(view.nargs)) {
         char buf[256];
@@ -93,13 +104,13 @@ extern "C" int sid_leaf_hull_noalloc(sid_engine* engine, int lemma_id, const dou
                       (unsigned long long)n, view.nargs, (unsigned long long)kMaxItemVars);
         return fail_status(SID_ERR_CAPACITY, buf);
     }
-    if(view.device < 0 || view.device >= kMaxDevices) return fail_status(SID_ERR_INVALID, "device id out of range");
 
     cudaError_t e = cudaSetDevice(view.device);
     if(e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
     unsigned long long* scratch = nullptr;
     {
-        // one-time set-up per device: the device address of the file-scope scratch array
+        // one-time set-up per device: the device address of the file-scope scratch array (kept for the life of
+        // the process; a device reset after this point is not supported, sid.h says so)
         std::lock_guard<std::mutex> lock(g_setup_mutex);
         if(!g_scratch_addr[view.device]) {
             void* p = nullptr;
@@ -110,7 +121,6 @@ extern "C" int sid_leaf_hull_noalloc(sid_engine* engine, int lemma_id, const dou
         scratch = g_scratch_addr[view.device];
     }
 
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     const std::uint64_t m = n * std::uint64_t(view.nargs);
     unsigned long long* lo = scratch + kHeaderWords;
     // the array keeps the previous call's contents: reset counters and accumulators

@@ -8,6 +8,9 @@ the reference's run_proof ("Starting proof <name>...") are attached to the files
 
   python export_lemmas.py [--reference DIR] [--out DIR] [--check]
 
+The reference tree is taken from --reference, else from the environment variable SID_REFERENCE_DIR, else
+from the mount point of the machine that holds the reference checkout (reference_dir()).
+
 --check regenerates into a temporary directory and fails if any committed file differs.
 This needs the reference sources, so it runs only where they are present.
 """
@@ -22,6 +25,12 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
+REFERENCE_MOUNT = "/root/reference"   # where the build machine mounts the reference checkout (read-only)
+
+
+def reference_dir():
+    """The reference checkout: SID_REFERENCE_DIR if set, else the build machine's mount point."""
+    return os.environ.get("SID_REFERENCE_DIR") or REFERENCE_MOUNT
 SOURCES = ["main", "top_packing", "one_subcontainer", "two_subcontainer", "three_subcontainer",
            "four_subcontainer", "five_subcontainer", "six_subcontainer", "seven_subcontainer",
            "more_subcontainers"]
@@ -96,10 +105,12 @@ def export(reference, out_dir, build_dir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None)
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--check", action="store_true")
     args = ap.parse_args()
+    if args.reference is None:
+        args.reference = reference_dir()
     build_dir = os.path.join(HERE, "_build")
     if args.check:
         tmp = tempfile.mkdtemp(prefix="sid_check_")

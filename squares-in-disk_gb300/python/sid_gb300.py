@@ -25,9 +25,11 @@ EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "si
             "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc", "sid_server_opts_default",
             "sid_server_create", "sid_server_destroy", "sid_submit", "sid_request_poll", "sid_request_wait",
             "sid_request_criticals", "sid_request_release", "sid_eval_batch_profile", "sid_eval_batch_profile_read",
-            "sid_lemma_autotune", "sid_prove_resume", "sid_lemma_batch_order"]
+            "sid_lemma_autotune", "sid_prove_resume", "sid_lemma_batch_order", "sid_eval_batch_plain_device",
+            "sid_lemma_operands", "sid_eval_operands_device", "sid_debug_inject_failure"]
 
 PRECISION_PLAIN, PRECISION_FP32, PRECISION_TUNED = 0, 1, 2
+INJECT_ALLOC, INJECT_LAUNCH = 1, 2
 BATCH_ORDER_AUTO, BATCH_ORDER_ON, BATCH_ORDER_OFF = 0, 1, 2
 MAX_LEVELS = 16
 REQ_PENDING, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
@@ -67,20 +69,23 @@ class SidProveOpts(ctypes.Structure):
 class SidServerOpts(ctypes.Structure):
     _fields_ = [("memory_budget_bytes", ctypes.c_uint64), ("step_elements", ctypes.c_int64),
                 ("precision", ctypes.c_int32), ("generation_count", ctypes.c_uint32),
-                ("max_criticals_per_request", ctypes.c_uint64), ("max_requests_per_lane", ctypes.c_uint32)]
+                ("max_criticals_per_request", ctypes.c_uint64), ("max_requests_per_lane", ctypes.c_uint32),
+                ("max_iterations_per_node", ctypes.c_int32), ("iteration_volume_criterion", ctypes.c_float),
+                ("iteration_single_dimension_criterion", ctypes.c_float)]
 
 
 class SidRequestStatus(ctypes.Structure):
     _fields_ = [("state", ctypes.c_int32), ("proved", ctypes.c_int32), ("num_cuboids", ctypes.c_uint64),
                 ("num_leaf_cuboids", ctypes.c_uint64), ("num_critical_cuboids", ctypes.c_uint64),
                 ("escalated", ctypes.c_uint64), ("criticals_stored", ctypes.c_uint64),
-                ("seconds_queued", ctypes.c_double), ("seconds_to_verdict", ctypes.c_double)]
+                ("seconds_queued", ctypes.c_double), ("seconds_to_verdict", ctypes.c_double),
+                ("num_repeated_nodes", ctypes.c_uint64)]
 
     def as_dict(self):
         return dict(state=self.state, proved=bool(self.proved), cuboids=self.num_cuboids,
                     leaves=self.num_leaf_cuboids, criticals=self.num_critical_cuboids, escalated=self.escalated,
                     stored=self.criticals_stored, seconds_queued=self.seconds_queued,
-                    seconds_to_verdict=self.seconds_to_verdict)
+                    seconds_to_verdict=self.seconds_to_verdict, repeated=self.num_repeated_nodes)
 
 
 class SidTuning(ctypes.Structure):
@@ -124,6 +129,14 @@ def load(path=LIB_PATH):
     L.sid_eval_batch_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p]
+    L.sid_eval_batch_plain_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p]
+    L.sid_lemma_operands.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
+    L.sid_eval_operands_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]
+    L.sid_debug_inject_failure.argtypes = [ctypes.c_int, ctypes.c_int64]
     L.sid_leaf_hull_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.sid_server_opts_default.argtypes = [ctypes.POINTER(SidServerOpts)]
@@ -149,6 +162,12 @@ def load(path=LIB_PATH):
 def _check(status):
     if status != SID_OK:
         raise SidError(status, load().sid_last_error().decode())
+
+
+def inject_failure(kind, countdown):
+    """Arm (countdown > 0) or disarm (0) a host-side failure of the countdown-th following device allocation
+    (INJECT_ALLOC) or kernel launch (INJECT_LAUNCH), see sid_debug_inject_failure."""
+    _check(load().sid_debug_inject_failure(kind, countdown))
 
 
 def lemma_ir(name):
@@ -283,6 +302,40 @@ class Engine:
         _check(self.L.sid_eval_batch_device(self.h, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr,
                                             verdict_ptr, stream))
 
+    def eval_batch_plain_device(self, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr, verdict_ptr, stream=0):
+        """The all-double batch evaluation (sid_eval_batch_plain_device) on device buffers."""
+        _check(self.L.sid_eval_batch_plain_device(self.h, lemma_id, lo_ptr, hi_ptr, n, out_lo_ptr, out_hi_ptr,
+                                                  verdict_ptr, stream))
+
+    def operand_count(self, lemma_id):
+        """Number of expressions the lemma's constraints compare (sid_lemma_operands)."""
+        k = ctypes.c_uint32()
+        _check(self.L.sid_lemma_operands(self.h, lemma_id, ctypes.byref(k)))
+        return k.value
+
+    def eval_operands_device(self, lemma_id, lo_ptr, hi_ptr, n, use_float, out_ptr, und_ptr, stream=0):
+        """Interval endpoints of the compared expressions on device boxes (sid_eval_operands_device): operand j
+        of box i at out[2*(j*n + i)] (lo) and out[2*(j*n + i) + 1] (hi), und[j*n + i]."""
+        _check(self.L.sid_eval_operands_device(self.h, lemma_id, lo_ptr, hi_ptr, n, 1 if use_float else 0, out_ptr,
+                                               und_ptr, stream))
+
+    def eval_operands(self, lemma_id, lo, hi, use_float):
+        """Host convenience over eval_operands_device: lo, hi (nargs, n) float64 -> (lohi (n, k, 2), und (n, k)),
+        the layout of the oracle's eval_operands. Needs torch for the device buffers."""
+        import torch
+        k = self.operand_count(lemma_id)
+        n = lo.shape[1]
+        d_lo = torch.from_numpy(np.ascontiguousarray(lo, dtype=np.float64)).cuda()
+        d_hi = torch.from_numpy(np.ascontiguousarray(hi, dtype=np.float64)).cuda()
+        out = torch.empty((max(k, 1), n, 2), dtype=torch.float64, device="cuda")
+        und = torch.empty((max(k, 1), n), dtype=torch.int8, device="cuda")
+        stream = torch.cuda.current_stream()
+        self.eval_operands_device(lemma_id, d_lo.data_ptr(), d_hi.data_ptr(), n, use_float, out.data_ptr(),
+                                  und.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        o = out.cpu().numpy()[:k].transpose(1, 0, 2).copy()
+        u = und.cpu().numpy()[:k].T.copy()
+        return o, u
 
     def autotune(self, lemma_id, max_seconds=5.0):
         """Choose the precision form's step size and float-pass levels for a lemma (sid_lemma_autotune)."""
@@ -322,7 +375,7 @@ class Server:
     """The served form (sid_server_*): requests of whole lemmas or sub-boxes, continuously batched per lemma."""
 
     def __init__(self, engine, precision=PRECISION_FP32, memory_budget=0, step_elements=0, generations=8,
-                 max_criticals=1024, max_requests_per_lane=0):
+                 max_criticals=1024, max_requests_per_lane=0, max_iterations=1):
         self.engine = engine
         self.L = engine.L
         o = SidServerOpts()
@@ -336,6 +389,7 @@ class Server:
         o.max_criticals_per_request = max_criticals
         if max_requests_per_lane:
             o.max_requests_per_lane = max_requests_per_lane
+        o.max_iterations_per_node = max_iterations
         h = ctypes.c_void_p()
         _check(self.L.sid_server_create(engine.h, ctypes.byref(o), ctypes.byref(h)))
         self.h = h

@@ -3,20 +3,25 @@
 
 For each lemma, on N seeded sampled leaves (synthetic boxes inside the lemma's root box, as in bench.py),
 every expression the constraints compare at run time is evaluated
-  * in float with outward rounding (the precision form's first pass: the CPU oracle's float evaluator),
-  * in double with outward rounding (the plain form: the oracle's double evaluator),
+  * in float with outward rounding (the precision form's first pass),
+  * in double with outward rounding (the plain form),
   * at 256 bits (tests/mp_judge.py, the "MPFR judge") on the first M of those leaves.
+The float and double intervals come from the GPU engine's endpoint dump (sid_eval_operands_device,
+--source device) or from the CPU oracle's evaluators (--source oracle); the GPU tests require the two to be
+equal bit for bit on these leaves.
 Reported per lemma: the mean and maximum interval-width ratio float/double and float/256-bit and
 double/256-bit (over expression values with positive finite widths), the number of enclosure violations
 (256-bit not inside double, or double not inside float; must be 0) and of contradicted verdicts (a
 comparison float or double calls definitely true where the judge calls it definitely false, or the
 reverse; must be 0).
 
-    python tests/precision_report.py [--leaves 100000] [--judge 10000] [--jobs 8] [--out FILE.json]
+    python tests/precision_report.py [--source oracle|device] [--leaves 100000] [--judge 10000] [--jobs 8]
+                                     [--out FILE.json]
 """
 import argparse
 import json
 import math
+import multiprocessing
 import os
 import sys
 from concurrent.futures import ProcessPoolExecutor
@@ -43,7 +48,8 @@ def _judge_chunk(args):
     return out
 
 
-def lemma_report(name, leaves, judge_leaves, jobs=1):
+def lemma_report(name, leaves, judge_leaves, jobs=1, engine=None):
+    """engine: a sid_gb300.Engine whose endpoint dump supplies the float and double intervals (else the oracle)."""
     import mp_judge
     import oracle_py
     import sid_gb300 as sid
@@ -59,8 +65,13 @@ def lemma_report(name, leaves, judge_leaves, jobs=1):
     cmp_nodes = [n for n in judge.L.nodes if n.op in ("lt", "le", "gt", "ge", "eq", "ne") and n.lb != n.ub]
     uniq = sorted({nid for nid in ops} - trivial)
     pos = {nid: ops.index(nid) for nid in uniq}
-    f32, u32 = oracle_py.eval_operands(ir, lo, hi, True)
-    f64, u64 = oracle_py.eval_operands(ir, lo, hi, False)
+    if engine is not None:
+        lid = engine.register(ir)
+        f32, u32 = engine.eval_operands(lid, lo, hi, True)
+        f64, u64 = engine.eval_operands(lid, lo, hi, False)
+    else:
+        f32, u32 = oracle_py.eval_operands(ir, lo, hi, True)
+        f64, u64 = oracle_py.eval_operands(ir, lo, hi, False)
 
     def widths(a):
         return a[..., 1] - a[..., 0]
@@ -77,7 +88,8 @@ def lemma_report(name, leaves, judge_leaves, jobs=1):
     bounds = np.linspace(0, m, chunks + 1).astype(int)
     tasks = [(ir, lo[:, a:b], hi[:, a:b], uniq) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
     if jobs > 1:
-        with ProcessPoolExecutor(max_workers=jobs) as ex:
+        # spawned workers: a process forked after CUDA was initialised must not run
+        with ProcessPoolExecutor(max_workers=jobs, mp_context=multiprocessing.get_context("spawn")) as ex:
             parts = list(ex.map(_judge_chunk, tasks))
     else:
         parts = [_judge_chunk(t) for t in tasks]
@@ -118,7 +130,8 @@ def lemma_report(name, leaves, judge_leaves, jobs=1):
         return {"mean": float(np.mean(r)) if len(r) else None, "max": float(np.max(r)) if len(r) else None,
                 "values": int(len(r))}
 
-    return {"lemma": name, "leaves": leaves, "judged_leaves": m, "expressions": len(uniq),
+    return {"lemma": name, "endpoints": "device" if engine is not None else "oracle", "leaves": leaves,
+            "judged_leaves": m, "expressions": len(uniq),
             "comparisons": len(cmp_nodes),
             "width_ratio_f32_over_f64": stats(r3264), "width_ratio_f32_over_mp256": stats(r32mp),
             "width_ratio_f64_over_mp256": stats(r64mp),
@@ -132,19 +145,24 @@ def main():
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--lemmas", nargs="*")
     ap.add_argument("--out")
+    ap.add_argument("--source", choices=["oracle", "device"], default="oracle",
+                    help="float and double endpoints from the CPU oracle or from the GPU engine's dump")
     args = ap.parse_args()
     import oracle_py
     import sid_gb300 as sid
     oracle_py.build()
+    engine = sid.Engine(0) if args.source == "device" else None
     names = args.lemmas or sid.lemma_names()
     rows = []
     for name in names:
-        r = lemma_report(name, args.leaves, args.judge, args.jobs)
+        r = lemma_report(name, args.leaves, args.judge, args.jobs, engine=engine)
         rows.append(r)
         print(json.dumps(r), flush=True)
     if args.out:
         with open(args.out, "w") as f:
-            json.dump({"seed": SEED, "rows": rows}, f, indent=1)
+            json.dump({"seed": SEED, "endpoints": args.source, "rows": rows}, f, indent=1)
+    if engine is not None:
+        engine.close()
     return 0
 
 

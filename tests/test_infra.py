@@ -68,10 +68,13 @@ def test_fingerprints_match_cpp_and_python():
 
 def test_lemma_ir_matches_unchanged_reference_sources():
     """The committed IR is what the reference's unchanged src/*.cpp produce with this front end."""
-    if not os.path.isdir("/root/reference/src"):
-        pytest.skip("reference sources not present")
-    r = subprocess.run([sys.executable, os.path.join(sid.PKG, "lemmas", "export_lemmas.py"), "--check"],
-                       capture_output=True, text=True)
+    sys.path.insert(0, os.path.join(sid.PKG, "lemmas"))
+    import export_lemmas
+    ref = export_lemmas.reference_dir()
+    if not os.path.isdir(os.path.join(ref, "src")):
+        pytest.skip("reference sources not present (set SID_REFERENCE_DIR)")
+    r = subprocess.run([sys.executable, os.path.join(sid.PKG, "lemmas", "export_lemmas.py"), "--check",
+                        "--reference", ref], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
 
 

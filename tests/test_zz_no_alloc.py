@@ -144,3 +144,18 @@ def test_leaf_hull_noalloc_rejects_oversized_calls(engine):
         engine.leaf_hull_noalloc(lid, small.data_ptr(), n, small.data_ptr(), flags.data_ptr(), 0)
     assert e.value.status == -7
     assert "allocation-free limit" in str(e.value)
+
+
+def test_leaf_hull_noalloc_empty_call_and_float_lemmas(engine):
+    """An empty call writes 0 leaves; float lemmas are rejected (as sid_eval_batch rejects them)."""
+    lid = engine.register(sid.lemma_ir("pos_neg1_sat"))
+    leaves = torch.full((1,), 12345, dtype=torch.int64, device="cuda")
+    engine.leaf_hull_noalloc(lid, 0, 0, 0, 0, leaves.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert int(leaves.item()) == 0
+    flid = engine.register(sid.lemma_ir("expected_critical2_f32"))
+    small = torch.zeros(16, dtype=torch.float64, device="cuda")
+    flags = torch.zeros(16, dtype=torch.uint8, device="cuda")
+    with pytest.raises(sid.SidError) as e:
+        engine.leaf_hull_noalloc(flid, small.data_ptr(), 1, small.data_ptr(), flags.data_ptr(), 0)
+    assert e.value.status == -6
