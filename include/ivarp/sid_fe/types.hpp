@@ -89,7 +89,8 @@ struct ProverSettings {
     int cuda_threads_per_block = 256;
     std::chrono::milliseconds start_progress_after{8000};
     std::chrono::milliseconds progress_every{2000};
-    /// Re-iteration limit per node; values <= 1 disable re-iteration (the published proofs use 1).
+    /// Passes over the static splits per queue element (<= 1: one pass, as the published proofs use); -1 (unset):
+    /// the reference CPU core's default of 4.
     int max_iterations_per_node = -1;
     float iteration_volume_criterion = -1.f;
     float iteration_single_dimension_criterion = -1.f;

@@ -375,10 +375,62 @@ template<class T> struct Evaluator {
 
 enum BoundID { NONE = 0, LB = 1, UB = 2, BOTH = 3, EMPTY = 4 };
 
+/// The constraints of each row in the engine's evaluation order (the code generator's row_order): repeatedly the
+/// constraint whose not yet evaluated nodes weigh least (square root and quotient 12, arc cosine 40, product 2,
+/// integer power 3, other operations 1, arguments and constants 0; ties in table order). A row holds iff every
+/// constraint holds, so the order changes no result, only the work done before the first refuted constraint.
+std::vector<std::vector<int>> device_row_order(const LemmaIR& L) {
+    auto weight = [&](std::size_t nid) {
+        switch(L.nodes[nid].op) {
+            case NodeOp::Arg: case NodeOp::Const: case NodeOp::BoolConst: return 0;
+            case NodeOp::Sqrt: case NodeOp::Div: return 12;
+            case NodeOp::Acos: return 40;
+            case NodeOp::Mul: return 2;
+            case NodeOp::Pow: return 3;
+            default: return 1;
+        }
+    };
+    std::vector<std::vector<int>> out(L.rows.size());
+    for(std::size_t r = 0; r < L.rows.size(); ++r) {
+        const std::vector<int>& cons = L.rows[r];
+        std::vector<std::vector<char>> in(cons.size(), std::vector<char>(L.nodes.size(), 0));
+        for(std::size_t c = 0; c < cons.size(); ++c) {
+            std::vector<int> stack{L.constraints[std::size_t(cons[c])]};
+            while(!stack.empty()) {
+                const int nid = stack.back();
+                stack.pop_back();
+                if(in[c][std::size_t(nid)]) continue;
+                in[c][std::size_t(nid)] = 1;
+                for(int ch : L.nodes[std::size_t(nid)].ch) stack.push_back(ch);
+            }
+        }
+        std::vector<char> done(L.nodes.size(), 0), taken(cons.size(), 0);
+        for(std::size_t k = 0; k < cons.size(); ++k) {
+            std::size_t best = cons.size();
+            long best_w = 0;
+            for(std::size_t c = 0; c < cons.size(); ++c) {
+                if(taken[c]) continue;
+                long w = 0;
+                for(std::size_t nid = 0; nid < L.nodes.size(); ++nid) if(in[c][nid] && !done[nid]) w += weight(nid);
+                if(best == cons.size() || w < best_w) { best = c; best_w = w; }
+            }
+            taken[best] = 1;
+            out[r].push_back(cons[best]);
+            for(std::size_t nid = 0; nid < L.nodes.size(); ++nid) if(in[best][nid]) done[nid] = 1;
+        }
+    }
+    return out;
+}
+
+// the oracle tests each row in the reference's table order unless set_device_row_order(true) selects the
+// engine's order (the op-counting build uses it to count the engine's operations)
+std::atomic<bool> g_device_row_order{false};
+
 template<class T> struct Prover {
     const LemmaIR& L;
     Evaluator<T> ev;
     int nb;
+    std::vector<std::vector<int>> rows;   // constraint ids of each row, in the order they are tested
     // propagation state (IndexQueueSet + IteratedRecursivePropInfo)
     std::vector<int> ring;
     std::vector<char> present, unstable;
@@ -387,6 +439,7 @@ template<class T> struct Prover {
     std::size_t qb = 0, qe = 0, qn = 0;
 
     explicit Prover(const LemmaIR& l) : L(l), ev(l), nb(int(l.bounds.size())),
+        rows(g_device_row_order.load() ? device_row_order(l) : l.rows),
         ring(std::size_t(std::max(nb, 1))), present(std::size_t(std::max(nb, 1)), 0),
         unstable(std::size_t(std::max(nb, 1)), 0), rec(std::size_t(std::max(nb, 1)), 0) {}
 
@@ -478,7 +531,7 @@ template<class T> struct Prover {
     bool rows_ok(int r0, int r1, const Iv<T>* box) {
         ev.begin(box);
         for(int r = r0; r < r1; ++r) {
-            for(int ci : L.rows[std::size_t(r)]) {
+            for(int ci : rows[std::size_t(r)]) {
                 if(!ev.evalp(L.constraints[std::size_t(ci)]).ub) return false;
             }
         }
@@ -884,6 +937,12 @@ void count_ops(unsigned long long out[10]) {
 #else
     throw std::runtime_error("oracle: built without SIDO_COUNT_OPS");
 #endif
+}
+
+void set_device_row_order(bool on) { g_device_row_order.store(on); }
+
+std::vector<std::vector<int>> device_row_order(const std::string& ir) {
+    return device_row_order(sid::parse_lemma_ir(ir));
 }
 
 std::vector<int> operand_nodes(const std::string& ir) {

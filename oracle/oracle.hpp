@@ -96,6 +96,11 @@ void eval_operands(const std::string& ir, const double* lo, const double* hi, st
 /// call (additions/subtractions, multiplications, divisions, square roots, arc cosines), then reset.
 void count_ops(unsigned long long out[10]);   // per kind (see make_ops_table.py), double then float
 
+/// Test each constraint row in the engine's order (cheapest not yet evaluated constraint first) instead of the
+/// reference's table order: same results, the engine's operation counts.
+void set_device_row_order(bool on);
+std::vector<std::vector<int>> device_row_order(const std::string& ir);   // constraint ids per row, in that order
+
 /// Initial runtime box (2*nargs doubles).
 std::vector<double> root_box(const std::string& ir);
 

@@ -104,6 +104,26 @@ int sido_eval_operands(const char* ir, const double* lo, const double* hi, unsig
     }
 }
 
+/* Constraint order of rows in the oracle's provers created from now on: 1 the engine's, 0 the reference's. */
+int sido_set_device_row_order(int on) {
+    sido::set_device_row_order(on != 0);
+    return 0;
+}
+
+/* The engine's constraint order of row `row`: up to cap constraint ids into out; returns their number or -1. */
+int sido_device_row_order(const char* ir, int row, int* out, int cap) {
+    try {
+        const auto rows = sido::device_row_order(std::string(ir));
+        if(row < 0 || row >= int(rows.size())) return 0;
+        const auto& r = rows[std::size_t(row)];
+        for(std::size_t k = 0; k < r.size() && int(k) < cap; ++k) out[k] = r[k];
+        return int(r.size());
+    } catch(const std::exception& e) {
+        last_error = e.what();
+        return -1;
+    }
+}
+
 /* Op-counting build only: operations since the last call (add/sub, mul, div, sqrt, acos), ten counts: in
  * double, then in float; 0 or -1. */
 int sido_count_ops(unsigned long long* out) {

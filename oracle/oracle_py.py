@@ -120,6 +120,17 @@ def acos_bound_f32(x, up):
     return out
 
 
+def device_row_order(ir_text, row):
+    """Constraint ids of a row in the engine's evaluation order (cheapest not yet evaluated constraint first)."""
+    L = lib()
+    L.sido_device_row_order.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    out = np.zeros(1024, dtype=np.int32)
+    k = L.sido_device_row_order(ir_text.encode(), row, out.ctypes.data, len(out))
+    if k < 0:
+        raise RuntimeError(_err())
+    return [int(x) for x in out[:k]]
+
+
 def operand_nodes(ir_text):
     """Node ids of the expressions the constraints compare at run time (left, right per comparison)."""
     ids = np.zeros(4096, dtype=np.int32)

@@ -19,7 +19,7 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.environ.get("SID_BUILD_DIR") or os.path.join(HERE, "_build")   # another directory for variant builds
 GEN = os.path.join(BUILD, "gen")
 LIB = os.path.join(BUILD, "libsid.so")
 

@@ -158,6 +158,38 @@ def comparison_operands(L):
     return out
 
 
+# weights of the operations in the evaluation order below (directed-rounding square roots and quotients take
+# several instructions; arc cosines many)
+OP_WEIGHT = {"sqrt": 12, "div": 12, "acos": 40, "mul": 2, "pow": 3}
+
+
+def op_weight(n):
+    return 0 if n.op in ("arg", "const", "bconst") else OP_WEIGHT.get(n.op, 1)
+
+
+def row_order(L, r):
+    """The constraints of row r in evaluation order: repeatedly the one whose not yet evaluated nodes weigh least
+    (ties: table order). A row holds iff all its constraints hold, so the order changes no verdict; testing cheap
+    constraints first lets the first refuted one stop the row early at lower cost."""
+    cons = list(L.rows.get(r, []))
+    nodes = {}
+    for ci in cons:
+        acc, stack = set(), [L.constraints[ci]]
+        while stack:
+            nid = stack.pop()
+            if nid not in acc:
+                acc.add(nid)
+                stack.extend(L.nodes[nid].ch)
+        nodes[ci] = acc
+    done, order = set(), []
+    while cons:
+        ci = min(cons, key=lambda c: (sum(op_weight(L.nodes[x]) for x in nodes[c] - done), cons.index(c)))
+        order.append(ci)
+        cons.remove(ci)
+        done |= nodes[ci]
+    return order
+
+
 def tri_nn(n):
     return 1 if n.lb >= 0 else (0 if n.ub <= 0 else -1)
 
@@ -353,7 +385,7 @@ def hoist_plan(L, var, r0, r1):
             memo[nid] = frozenset(d)
         return memo[nid]
 
-    top = [L.constraints[ci] for r in range(r0, r1) for ci in L.rows.get(r, [])]
+    top = [L.constraints[ci] for r in range(r0, r1) for ci in row_order(L, r)]
     if not top:
         return None
     inv_top = [p for p in top if var not in deps(p)]
@@ -503,6 +535,9 @@ def generate(lemma):
         w("        }")
         w("    }")
     w("    template<class T> __device__ static int apply_bound(int k, Iv<T>* box);")
+    w("    template<int K, class T> __device__ static int apply_bound_c(Iv<T>* box);   // bound K, K known at compile time")
+    w("    // the bounds a change of the last variable queues first (upd_both of the last variable)")
+    w("    static constexpr std::uint64_t SEED_LAST = 0x%xull;" % mask(L.upd.get((L.nargs - 1, "both"), [])))
     w("    template<class T, bool ALL> __device__ static int rows_eval(int r0, int r1, const Iv<T>* box);")
     w("    template<class T> __device__ static int rows_status(int r0, int r1, const Iv<T>* box) {")
     w("        return rows_eval<T, true>(r0, r1, box);")
@@ -520,6 +555,7 @@ def generate(lemma):
     w("        return ((REST_ROWS >> r0) & ((1ull << (r1 - r0)) - 1)) != 0;")
     w("    }")
     w("    template<class T> __device__ static bool rows_cheap(int r0, int r1, const Iv<T>* box);")
+    w("    template<int R, class T> __device__ static bool row_cheap_c(const Iv<T>* box);   // rowc_R, R known at compile time")
     w("    template<class T> __device__ static bool rows_rest(int r0, int r1, const Iv<T>* box);")
     for r in range(L.nargs):
         w("    template<class T> __device__ static bool rowc_%d(const Iv<T>* box);" % r)
@@ -531,19 +567,26 @@ def generate(lemma):
     w("                                                      std::uint64_t stride, std::uint64_t i);")
     w("};")
     w("")
-    # bound functions
-    w("template<class T> __device__ int L::apply_bound(int k, Iv<T>* box) {")
-    w("    switch(k) {")
+    # bound functions: one per bound, dispatched at run time (apply_bound) or at compile time (apply_bound_c)
     for k, (tgt, d, fn, defined) in enumerate(L.bounds):
         e = Emitter(L)
-        e.indent = 2
+        e.indent = 1
         v = e.expr(fn, {})
-        w("    case %d: {" % k)
+        w("template<class T> __device__ __forceinline__ int bound_%d(Iv<T>* box) {" % k)
         out.extend(e.lines)
-        w("        return apply_to<%d, %s>(box[%d], %s);" % (d, "true" if defined else "false", tgt, v))
-        w("    }")
+        w("    return apply_to<%d, %s>(box[%d], %s);" % (d, "true" if defined else "false", tgt, v))
+        w("}")
+    w("template<class T> __device__ int L::apply_bound(int k, Iv<T>* box) {")
+    w("    switch(k) {")
+    for k in range(len(L.bounds)):
+        w("    case %d: return bound_%d<T>(box);" % (k, k))
     w("    default: return B_NONE;")
     w("    }")
+    w("}")
+    w("template<int K, class T> __device__ __forceinline__ int L::apply_bound_c(Iv<T>* box) {")
+    for k in range(len(L.bounds)):
+        w("    %sif constexpr(K == %d) return bound_%d<T>(box);" % ("" if k == 0 else "else ", k, k))
+    w("    %sreturn B_NONE;" % ("else " if L.bounds else ""))
     w("}")
     w("")
     for r in range(L.nargs):
@@ -551,7 +594,7 @@ def generate(lemma):
         w("    bool all = true;")
         e = Emitter(L)
         scope = {}
-        for ci in L.rows.get(r, []):
+        for ci in row_order(L, r):
             p = e.pred(L.constraints[ci], scope)
             e.emit("if(!%s.ub) return 0;" % p)
             e.emit("if constexpr(ALL) all = all && %s.lb;" % p)
@@ -565,7 +608,7 @@ def generate(lemma):
             w("template<class T> __device__ bool L::%s_%d(const Iv<T>* box) {" % (fname, r))
             e = Emitter(L)
             scope = {}
-            for ci in L.rows.get(r, []):
+            for ci in row_order(L, r):
                 if cheap_constraint(L, L.constraints[ci]) == cheap:
                     p = e.pred(L.constraints[ci], scope)
                     e.emit("if(!%s.ub) return false;" % p)
@@ -587,6 +630,12 @@ def generate(lemma):
         w("    return true;")
         w("}")
         w("")
+    w("template<int R, class T> __device__ __forceinline__ bool L::row_cheap_c(const Iv<T>* box) {")
+    for r in range(L.nargs):
+        w("    %sif constexpr(R == %d) return rowc_%d<T>(box);" % ("" if r == 0 else "else ", r, r))
+    w("    else return true;")
+    w("}")
+    w("")
     w("template<class T, bool ALL> __device__ int L::rows_eval(int r0, int r1, const Iv<T>* box) {")
     w("    int status = 2;")
     w("    for(int r = r0; r < r1; ++r) {")

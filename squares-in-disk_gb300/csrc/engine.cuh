@@ -218,6 +218,32 @@ template<class L, class T, bool DEFER> __device__ int propagate_packed(int arg, 
     return 0;
 }
 
+/// Lowest set bit of a non-zero mask, at compile time.
+__host__ __device__ constexpr int ctz64(std::uint64_t m) { return (m & 1ull) ? 0 : 1 + ctz64(m >> 1); }
+
+/// The start of a propagation whose seed (the bounds queued first, in increasing id order) is the compile-time
+/// mask SEED: the seed bounds are applied in queue order, dispatched at compile time, while each leaves the box
+/// unchanged. Until a bound changes the box nothing else is queued, so if a seed bound empties the box, or all
+/// of them leave it unchanged, that is the result of the whole propagation (1: empty, 0: not empty). Returns -1
+/// as soon as a seed bound changed the box without emptying it, or (with DEFER) before a seed bound of
+/// L::SLOW_BOUNDS: the caller then runs the full propagation from the original box, which repeats these
+/// applications first and continues exactly as it would have.
+template<class L, class T, bool DEFER, std::uint64_t SEED> __device__ __forceinline__ int propagate_seed(Iv<T>* box) {
+    if constexpr(SEED == 0) {
+        return 0;
+    } else {
+        constexpr int k = ctz64(SEED);
+        if constexpr(DEFER && ((L::SLOW_BOUNDS >> k) & 1ull)) {
+            return -1;
+        } else {
+            const int r = L::template apply_bound_c<k, T>(box);
+            if(r == B_EMPTY) return 1;
+            if(r != B_NONE) return -1;
+            return propagate_seed<L, T, DEFER, SEED & (SEED - 1)>(box);
+        }
+    }
+}
+
 /// Splitter::subrange (splitter.hpp:44-59): width (ub-lb)/n and points lb + i*w, all rounded down
 /// like the reference's global rounding mode; the last point is exactly ub.
 template<class T> __device__ __forceinline__ void split_child(T lb, T ub, int n, int i, T& lo, T& hi) {
@@ -374,15 +400,17 @@ template<class L, class T>
 __device__ __forceinline__ bool eval_child(const LevelArgs& a, const std::uint64_t item, const int c, Iv<T>* box,
                                            const bool float_rows) {
     constexpr int N = L::NARGS;
+    // the split variable is known only at run time: select it in an unrolled loop, so that every index into the
+    // box is a constant (an index computed at run time puts the box in local memory)
     #pragma unroll
     for(int v = 0; v < N; ++v) {
         double2 b = a.in_box[std::uint64_t(v) * a.in_stride + item];
         box[v] = {T(b.x), T(b.y), false};
-    }
-    {
-        T lo, hi;
-        split_child(box[a.var].lo, box[a.var].hi, a.nsub, c, lo, hi);
-        box[a.var] = {lo, hi, false};
+        if(v == a.var) {
+            T lo, hi;
+            split_child(box[v].lo, box[v].hi, a.nsub, c, lo, hi);
+            box[v] = {lo, hi, false};
+        }
     }
     bool ok = !propagate<L, T>(a.var, box, a.it_limit, a.rec_limit);
     if(ok && a.row_end > a.row_begin) {
@@ -909,6 +937,66 @@ template<class L, class T, bool DEFER> __device__ __forceinline__ void batch_res
     }
 }
 
+/// Stage 1 of the batch kernel for one cuboid per lane (all lanes of each warp call it; `valid` marks the lanes
+/// with cuboid i, whose input box is in `box`): the seed bounds decide most cuboids at once (emptied, or left
+/// unchanged); the others start over from their input box with the full propagation. Then the comparison-only
+/// constraints in the lemma's own type; outputs: the propagated box and, unless the cuboid goes on to stage 2
+/// (`push`) or to the deferred list (`defer`), its verdict. With DEFER a cuboid whose propagation reaches a slow
+/// bound is deferred, unless kInlineLanes lanes of its warp reached one (then they start over here together).
+template<class L, class T, bool DEFER> __device__ __forceinline__ void batch_stage1(const BatchArgs& a, const bool valid,
+                                                                                    const std::uint64_t i, Iv<T>* box,
+                                                                                    bool& push, bool& defer) {
+    constexpr int N = L::NARGS;
+    constexpr bool rest = ((L::REST_ROWS >> (N - 1)) & 1ull) != 0;
+    constexpr bool DEF = DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0;
+    const std::uint64_t st = a.stride ? a.stride : a.n;
+    int pr = 0;
+    if(valid) {
+        pr = propagate_seed<L, T, DEF, L::SEED_LAST>(box);
+        if(pr < 0) {
+            #pragma unroll
+            for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
+            if constexpr(DEF) {
+                pr = propagate_packed<L, T, true>(N - 1, box, N, 4);
+            } else {
+                pr = propagate<L, T>(N - 1, box, N, 4) ? 1 : 0;
+            }
+        }
+    }
+    if constexpr(DEF && !batch_inline(L::NARGS)) {
+        defer = pr == 2;
+    } else if constexpr(DEF) {
+        // a few lanes that reached a slow bound go to k_eval_batch_slow; when many of the warp's lanes did, they
+        // start over here together instead
+        const unsigned dm = __ballot_sync(0xffffffffu, pr == 2);
+        if(__popc(dm) >= kInlineLanes) {
+            if(pr == 2) {
+                #pragma unroll
+                for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
+                pr = propagate<L, T>(N - 1, box, N, 4) ? 1 : 0;
+            }
+        } else {
+            defer = pr == 2;
+        }
+    }
+    if(valid && !defer) {
+        std::int8_t vd = 0;
+        if(pr == 1) {
+            vd = 1;
+        } else if(!L::template row_cheap_c<N - 1, T>(box)) {
+            vd = 2;
+        } else if(rest) {
+            push = true;
+        }   // else every constraint of the row only compares, and the test above was the full one
+        if(!push) a.verdict[i] = vd;
+        #pragma unroll
+        for(int v = 0; v < N; ++v) {
+            a.out_lo[std::uint64_t(v) * st + i] = double(box[v].lo);
+            a.out_hi[std::uint64_t(v) * st + i] = double(box[v].hi);
+        }
+    }
+}
+
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
 /// (it_limit = nargs, rec_limit = 4) and test all constraints; the verdict is the double one bit for bit.
 /// Two stages per block of SID_BATCH_TILES tiles of 128 cuboids: (1) one thread per cuboid loads,
@@ -933,7 +1021,6 @@ template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, ba
     __shared__ int qn;
     const std::uint64_t st = a.stride ? a.stride : a.n;
     const std::uint64_t first = std::uint64_t(blockIdx.x) * (128u * SID_BATCH_TILES);
-    const bool rest = L::has_rest(N - 1, N);
     unsigned long long n_double = 0;
     if(threadIdx.x == 0) qn = 0;
     __syncthreads();
@@ -945,49 +1032,12 @@ template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, ba
         bool push = false, defer = false;
         std::uint64_t i = 0;
         Iv<T> box[N];
-        int pr = 0;
         if(valid) {
             i = a.order ? std::uint64_t(a.order[t]) : t;
             #pragma unroll
             for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
-            if constexpr(DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0) {
-                pr = propagate_packed<L, T, true>(N - 1, box, N, 4);
-            } else {
-                pr = propagate<L, T>(N - 1, box, N, 4) ? 1 : 0;
-            }
         }
-        if constexpr(DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0 && !batch_inline(L::NARGS)) {
-            defer = pr == 2;
-        } else if constexpr(DEFER && L::NBOUNDS <= 16 && L::SLOW_BOUNDS != 0) {
-            // a few lanes that reached a slow bound go to k_eval_batch_slow; when many of the warp's lanes
-            // did, they start over here together instead
-            const unsigned dm = __ballot_sync(0xffffffffu, pr == 2);
-            if(__popc(dm) >= kInlineLanes) {
-                if(pr == 2) {
-                    #pragma unroll
-                    for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
-                    pr = propagate<L, T>(N - 1, box, N, 4) ? 1 : 0;
-                }
-            } else {
-                defer = pr == 2;
-            }
-        }
-        if(valid && !defer) {
-            std::int8_t vd = 0;
-            if(pr == 1) {
-                vd = 1;
-            } else if(!L::template rows_cheap<T>(N - 1, N, box)) {
-                vd = 2;
-            } else if(rest) {
-                push = true;
-            }   // else every constraint of the row only compares, and the test above was the full one
-            if(!push) a.verdict[i] = vd;
-            #pragma unroll
-            for(int v = 0; v < N; ++v) {
-                a.out_lo[std::uint64_t(v) * st + i] = double(box[v].lo);
-                a.out_hi[std::uint64_t(v) * st + i] = double(box[v].hi);
-            }
-        }
+        batch_stage1<L, T, DEFER>(a, valid, i, box, push, defer);
         if constexpr(DEFER) defer_cuboids(a, defer, i);
         const unsigned m = __ballot_sync(0xffffffffu, push);
         if(m) {

@@ -12,7 +12,7 @@ import numpy as np
 
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REPO = os.path.dirname(PKG)
-LIB_PATH = os.path.join(PKG, "_build", "libsid.so")
+LIB_PATH = os.path.join(os.environ.get("SID_BUILD_DIR") or os.path.join(PKG, "_build"), "libsid.so")
 LEMMA_DIR = os.path.join(PKG, "lemmas")
 KAT_DIR = os.path.join(REPO, "tests", "golden", "kat")
 

@@ -3,7 +3,8 @@
 multiplications, divisions, square roots, arc cosines) per cuboid, counted by the op-counting build of the
 CPU oracle (oracle/_build/liboracle_ops.so, -DSIDO_COUNT_OPS):
   * "batch": leaf evaluation (propagation after a change of the last variable, all constraints) of a
-    seeded sample of bench.py's synthetic batch, per lemma, in the device's order: double operations with
+    seeded sample of bench.py's synthetic batch, per lemma, in the device's order (each row's constraints
+    cheapest first, as the code generator emits them): double operations with
     the constraints tested in float first and in double only where float does not refute them ("batch_f32":
     the float operations of that order; "batch_plain": double operations of the all-double order);
   * "proof": whole plain proofs of the lemmas the oracle proves in seconds, per cuboid considered.
@@ -35,6 +36,7 @@ def main():
     import sid_gb300 as sid
     oracle_py.build()
     L = ctypes.CDLL(os.path.join(REPO, "oracle", "_build", "liboracle_ops.so"))
+    L.sido_set_device_row_order(1)       # count the engine's operations: its constraint order within each row
     counts = (ctypes.c_ulonglong * 10)()
 
     def take(which="f64"):

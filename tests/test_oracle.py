@@ -1,6 +1,7 @@
 """CPU tests of the oracle against the reference's golden numbers (published counts, known-answer tests)."""
 import json
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -93,3 +94,22 @@ def test_oracle_shards_sum_to_the_whole_proof(oracle, name, parts):
     res = [oracle.prove(ir, part=(i, parts)) for i in range(parts)]
     assert [sum(r["cuboids"] for r in res), sum(r["leaves"] for r in res)] == PUBLISHED[name]
     assert all(r["cuboids"] > 0 for r in res)
+
+
+def test_oracle_row_order_is_the_code_generators(oracle):
+    """The oracle's copy of the engine's constraint order (used to count the engine's operations) equals the
+    order the code generator emits, for every row of every lemma and known-answer system."""
+    import tempfile
+    sys.path.insert(0, os.path.join(REPO, "squares-in-disk_gb300", "csrc"))
+    import codegen
+    names = [(n, sid.lemma_ir(n)) for n in sid.lemma_names()]
+    names += [(f[:-6], open(os.path.join(sid.KAT_DIR, f)).read()) for f in sorted(os.listdir(sid.KAT_DIR))]
+    for name, ir in names:
+        with tempfile.NamedTemporaryFile("w", suffix=".sidir", delete=False) as f:
+            f.write(ir)
+        try:
+            L = codegen.Lemma(f.name)
+        finally:
+            os.unlink(f.name)
+        for r in range(L.nargs):
+            assert oracle.device_row_order(ir, r) == codegen.row_order(L, r), (name, r)
