@@ -112,6 +112,14 @@ typedef struct sid_prove_opts {
                                            i % part_count == part_index. The parts' counts sum to the whole
                                            proof's and their criticals together are the whole proof's, so
                                            parts can run on separate GPUs or processes. 0 or 1: whole proof. */
+    uint32_t device_loop_blocks;        /* no counterpart in the reference: > 0 runs the whole proof in one
+                                           persistent kernel on this many co-resident 128-thread blocks (at
+                                           most the device's limit for that kernel), with no host round trip
+                                           between levels or steps; 0 (default) drives each level from the
+                                           host. Same counts and criticals either way. Proofs that need
+                                           re-iteration, checkpoints or progress callbacks use the host loop; a
+                                           proof whose queue outgrows the loop's preallocated room is redone by
+                                           the host loop. */
 } sid_prove_opts;
 
 /* Fill `opts` with the defaults above. */

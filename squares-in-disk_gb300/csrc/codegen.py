@@ -499,6 +499,7 @@ def generate(lemma):
     w = out.append
     w("// Generated by csrc/codegen.py from lemmas/%s -- do not edit." % os.path.basename(L.path))
     w('#include "engine.cuh"')
+    w('#include "proof_loop.cuh"')
     w('#include "acos.cuh"')
     w("")
     w("namespace sid {")
@@ -700,6 +701,10 @@ def generate(lemma):
     w("static cudaError_t eval_batch_plain(const BatchArgs& a, cudaStream_t s) {")
     w("    return launch_eval_batch_plain<L, %s>(a, s);" % T_plain)
     w("}")
+    w("static cudaError_t proof_loop(const LoopArgs& a, unsigned blocks, cudaStream_t s) {")
+    w("    return launch_proof_loop<L, %s>(a, blocks, s);" % T_plain)
+    w("}")
+    w("static int proof_loop_occupancy() { return sid::proof_loop_occupancy<L, %s>(); }" % T_plain)
     w("static cudaError_t eval_operands(int use_float, const double* lo, const double* hi, std::uint64_t n,")
     w("                                 std::uint64_t stride, double2* o, std::int8_t* u, cudaStream_t s) {")
     w("    return launch_eval_operands<L, %s>(use_float, lo, hi, n, stride, o, u, s);" % T_plain)
@@ -717,7 +722,8 @@ def generate(lemma):
             "&{0}::filter_f32, &{0}::level_esc, &{0}::hoist_values, &{0}::prelude_f32, &{0}::filter_hoisted".format(ns))
     w("const LemmaKernels kernels_%s = {\"%s\", 0x%016xull, %d, %d, %s, &%s::level, &%s::root_box, &%s::eval_batch, %s," % (
         ns, L.slug, L.fingerprint, L.nargs, len(L.bounds), "true" if L.numtype == "f32" else "false", ns, ns, ns, prec))
-    w("    &%s::eval_batch_plain, %d, &%s::eval_operands};" % (ns, len(operands), ns))
+    w("    &%s::eval_batch_plain, %d, &%s::eval_operands, &%s::proof_loop, &%s::proof_loop_occupancy};" % (
+        ns, len(operands), ns, ns, ns))
     w("")
     w("} // namespace sid")
     return ns, "\n".join(out) + "\n"

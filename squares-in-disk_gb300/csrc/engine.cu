@@ -40,6 +40,7 @@
 #include "engine.cuh"
 #include "engine_internal.hpp"
 #include "lemma_ir.hpp"
+#include "proof_loop.cuh"
 #include "serve_plan.hpp"
 
 namespace sid {
@@ -665,8 +666,8 @@ struct Lane {
     }
 
     /// Admit a request: device slot, frontier queue, critical store; then its root partition (whole
-    /// lemma) or its sub-boxes as depth-0 elements.
-    void admit(Request* r) {
+    /// lemma; left to the device proof loop with root_on_device) or its sub-boxes as depth-0 elements.
+    void admit(Request* r, bool root_on_device = false) {
         int slot = -1;
         for(int i = 0; i < max_slots; ++i) {
             if(!slot_req[std::size_t(i)]) { slot = i; break; }
@@ -674,15 +675,35 @@ struct Lane {
         if(slot < 0) fail(SID_ERR_CAPACITY, "no free request slot");
         r->slot = slot;
         slot_req[std::size_t(slot)] = r;
-        r->qcap = initial_queue_cap(*r);
-        r->qbox.reserve_on(std::size_t(n) * r->qcap, st);
-        r->qdepth.reserve_on(r->qcap, st);
+        double2* qbox = nullptr;
+        std::uint8_t* qdepth = nullptr;
+        if(root_on_device) {
+            // the device loop's queue belongs to the lane and is reused by its proofs
+            r->qcap = loop_queue_cap();
+            if(loop_qcap < r->qcap) {
+                loop_qbox.release();
+                loop_qdepth.release();
+                loop_qcap = 0;
+                loop_qbox.reserve(std::size_t(n) * r->qcap);
+                loop_qdepth.reserve(r->qcap);
+                loop_qcap = r->qcap;
+            }
+            r->qcap = loop_qcap;
+            qbox = loop_qbox.p;
+            qdepth = loop_qdepth.p;
+        } else {
+            r->qcap = initial_queue_cap(*r);
+            r->qbox.reserve_on(std::size_t(n) * r->qcap, st);
+            r->qdepth.reserve_on(r->qcap, st);
+            qbox = r->qbox.p;
+            qdepth = r->qdepth.p;
+        }
         r->crit.reserve_on(std::max<std::uint64_t>(r->crit_cap, 1) * 2 * std::uint64_t(n), st);
         r->bytes = initial_bytes(*r);
         ReqDev& h = req_host[std::size_t(slot)];
         h = ReqDev{};
-        h.qbox = r->qbox.p;
-        h.qdepth = r->qdepth.p;
+        h.qbox = qbox;
+        h.qdepth = qdepth;
         h.qcap = r->qcap;
         h.crit = r->crit.p;
         h.crit_cap = r->crit_cap;
@@ -718,8 +739,9 @@ struct Lane {
             cuda_check(cudaMemsetAsync(r->qdepth.p, 0, std::size_t(r->nboxes), st), "sub-box depth");
         }
         cuda_check(cudaMemcpyAsync(req_dev.p + slot, &h, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
+        if(root_on_device) return;   // the loop's own read-back gives the counts; no wait here
         cuda_check(cudaStreamSynchronize(st), "request slot");
-        if(r->full && !r->resume) {
+        if(r->full && !r->resume && !root_on_device) {
             root_part_index = r->part_index;
             root_part_count = r->part_count;
             run_dynamic(0, lem->root.p, 1, nullptr, nullptr, std::uint32_t(slot), 0, 1, true, 0);
@@ -727,6 +749,124 @@ struct Lane {
         }
         read_slots();
     }
+
+    // device proof loop: control words, a queue reused by its proofs, per-block scratch (cached, grown as needed)
+    DevBuf<LoopCtl> loop_ctl;
+    DevBuf<double2> loop_qbox;
+    DevBuf<std::uint8_t> loop_qdepth;
+    std::uint64_t loop_qcap = 0;
+    DevBuf<double2> lb_sbox[kLoopMaxLevels], lb_dbox[kLoopMaxLevels], lb_hull;
+    DevBuf<std::uint32_t> lb_selem[kLoopMaxLevels], lb_esc;
+    DevBuf<std::uint64_t> lb_spath[kLoopMaxLevels];
+    DevBuf<std::uint8_t> lb_ddepth[kLoopMaxLevels];
+    DevBuf<float2> lb_pbox;
+    DevBuf<float4> lb_psplit;
+    DevBuf<unsigned long long> lb_ctl;
+
+    static constexpr std::uint64_t kBlockListItems = 2048;       // items of one per-block list
+    static constexpr std::uint64_t kBlockEscChildren = 1 << 14;  // children per float-pass chunk of a block
+    static constexpr std::uint64_t kLoopQueueBytes = std::uint64_t(1) << 30;   // most the loop's queue may hold
+
+    /// Queue capacity for a device-loop proof: the root partition and one full step's children, twice over,
+    /// within kLoopQueueBytes.
+    std::uint64_t loop_queue_cap() const {
+        const std::uint64_t per = 16 * std::uint64_t(n) + 1;
+        const std::uint64_t want = 2 * std::max<std::uint64_t>(root_fanout, step_cap * fanout);
+        return std::max<std::uint64_t>(64, std::min(want, kLoopQueueBytes / per));
+    }
+
+    /// A whole-lemma request admitted with root_on_device (its queue is the lane's loop queue), proved entirely in
+    /// the device proof loop (proof_loop.cuh) on `blocks` co-resident blocks (clamped to the device's limit for the
+    /// kernel). Returns false if the queue or a list would have overflowed (the request's counts are then
+    /// incomplete; the caller redoes the proof on the host-driven loop); throws SID_ERR_TIMEOUT if a barrier gave up.
+    bool run_device_loop(Request* r, unsigned blocks) {
+        const int D = int(dyn.size()), S = int(stat.size());
+        if(D < 1 || D > kLoopMaxLevels || S > kLoopMaxLevels) fail(SID_ERR_UNSUPPORTED, "device loop: too many levels");
+        const int occ = lem->k->proof_loop_occupancy ? lem->k->proof_loop_occupancy() : 0;
+        if(occ <= 0) fail(SID_ERR_UNSUPPORTED, "device loop: the kernel cannot be resident");
+        const unsigned G = std::max(1u, std::min(blocks, unsigned(occ) * unsigned(std::max(sm_count, 1))));
+        LoopArgs la{};
+        la.req = req_dev.p;
+        la.tag = std::uint32_t(r->slot);
+        la.nargs = n;
+        la.n_dyn = D;
+        la.n_stat = S;
+        for(int d = 0; d < D; ++d) {
+            la.dyn[d] = LoopSplit{dyn[std::size_t(d)].arg, int(dyn[std::size_t(d)].initial), int(dyn[std::size_t(d)].subdivisions)};
+        }
+        for(int j = 0; j < S; ++j) la.stat[j] = LoopSplit{stat[std::size_t(j)].arg, 0, int(stat[std::size_t(j)].subdivisions)};
+        la.root = lem->root.p;
+        la.part_index = r->part_index;
+        la.part_count = r->part_count;
+        la.fp32 = fp32_first;
+        la.fp32_mask = fp32_mask;
+        la.step = step_cap;
+        la.max_steps = std::uint64_t(1) << 40;
+        la.step_box = step.box.p;
+        la.step_depth = step.depth.p;
+        la.step_tag = step.tag.p;
+        la.step_cap = step_cap;
+        la.hull = hull.p;
+        // root partition lists (grid-wide): the initial subdivisions' products
+        std::uint64_t root_items = 1, p_cap = 1;
+        for(int d = 1; d < D; ++d) {
+            root_items *= std::uint64_t(dyn[std::size_t(d - 1)].initial);
+            BoxList& l = dyn_level(std::size_t(d));
+            l.reserve(n, std::max(l.cap, root_items), false, false, true, true);
+            la.dl_box[d] = l.box.p; la.dl_depth[d] = l.depth.p; la.dl_tag[d] = l.tag.p; la.dl_cap[d] = l.cap;
+            p_cap = std::max(p_cap, l.cap);
+        }
+        // per-block lists of one element's levels
+        std::uint64_t bp_cap = 1, items = 1;
+        for(int j = 1; j < S; ++j) {
+            items = std::min(items * std::uint64_t(stat[std::size_t(j - 1)].subdivisions), kBlockListItems);
+            lb_sbox[j].reserve(std::size_t(G) * items * std::uint64_t(n));
+            lb_selem[j].reserve(std::size_t(G) * items);
+            lb_spath[j].reserve(std::size_t(G) * items);
+            la.bs_box[j] = lb_sbox[j].p; la.bs_elem[j] = lb_selem[j].p; la.bs_path[j] = lb_spath[j].p; la.bs_cap[j] = items;
+            bp_cap = std::max(bp_cap, items);
+        }
+        items = 1;
+        for(int d = 1; d < D; ++d) {
+            items = std::min(items * std::uint64_t(dyn[std::size_t(d - 1)].subdivisions), kBlockListItems);
+            lb_dbox[d].reserve(std::size_t(G) * items * std::uint64_t(n));
+            lb_ddepth[d].reserve(std::size_t(G) * items);
+            la.bd_box[d] = lb_dbox[d].p; la.bd_depth[d] = lb_ddepth[d].p; la.bd_cap[d] = items;
+            bp_cap = std::max(bp_cap, items);
+        }
+        lb_hull.reserve(std::size_t(G) * std::uint64_t(n));
+        lb_ctl.reserve(std::size_t(G) * kBlockCtlWords);
+        la.b_hull_box = lb_hull.p;
+        la.b_ctl = lb_ctl.p;
+        if(fp32_first) {
+            esc.reserve(kEscChunk);
+            pbox.reserve(std::size_t(n) * p_cap);
+            psplit.reserve(std::size_t(p_cap));
+            la.esc = esc.p; la.esc_cap = kEscChunk; la.pbox = pbox.p; la.psplit = psplit.p; la.p_cap = p_cap;
+            lb_pbox.reserve(std::size_t(G) * bp_cap * std::uint64_t(n));
+            lb_psplit.reserve(std::size_t(G) * bp_cap);
+            lb_esc.reserve(std::size_t(G) * kBlockEscChildren);
+            la.b_pbox = lb_pbox.p; la.b_psplit = lb_psplit.p; la.b_p_cap = bp_cap;
+            la.b_esc = lb_esc.p; la.b_esc_cap = kBlockEscChildren;
+        }
+        loop_ctl.reserve(1);
+        cuda_check(cudaMemsetAsync(loop_ctl.p, 0, sizeof(LoopCtl), st), "loop control");
+        la.ctl = loop_ctl.p;
+        launch_gate("device proof loop");
+        cuda_check(lem->k->proof_loop(la, G, st), "device proof loop launch");
+        LoopCtl c{};
+        ReqDev h{};
+        cuda_check(cudaMemcpyAsync(&c, loop_ctl.p, sizeof(LoopCtl), cudaMemcpyDeviceToHost, st), "loop control");
+        cuda_check(cudaMemcpyAsync(&h, req_dev.p + r->slot, sizeof(ReqDev), cudaMemcpyDeviceToHost, st), "request");
+        cuda_check(cudaStreamSynchronize(st), "device proof loop");
+        if(c.error == kLoopTimeout) fail(SID_ERR_TIMEOUT, "device proof loop: a grid barrier gave up");
+        // an append that did not fit is counted, not written; the proof is then redone on the host
+        if(c.error != kLoopOk || h.cnt[RC_OVERFLOW] != 0 || h.cnt[RC_QSIZE] != 0) return false;
+        std::memcpy(req_host[std::size_t(r->slot)].cnt, h.cnt, sizeof(h.cnt));
+        loop_steps = std::uint32_t(c.steps);
+        return true;
+    }
+    std::uint32_t loop_steps = 0;
 
     /// Drop a request's device state (after completion or failure).
     void release(Request* r) {
@@ -989,9 +1129,9 @@ struct Lane {
     }
 
     /// Make room in a request's queue before a step takes `taken` of its elements.
-    void ensure_queue(Request* r, std::uint64_t taken) {
+    void ensure_queue(Request* r, std::uint64_t taken, std::uint64_t at_least = 0) {
         const std::uint64_t qsize = queue_size(r);
-        const std::uint64_t need = plan::queue_need(qsize, taken, fanout);
+        const std::uint64_t need = std::max(plan::queue_need(qsize, taken, fanout), at_least);
         if(need <= r->qcap) return;
         const std::uint64_t ncap = plan::grow_capacity(r->qcap, need);
         DevBuf<double2> nb;
@@ -1370,7 +1510,20 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
         const auto t0 = Clock::now();
         auto last_cb = t0;
         bool first_done = false;
-        lane.admit(&r);
+        // the device proof loop takes the whole proof (root partition included) when asked for and when the proof
+        // needs nothing between steps from the host
+        const bool loop = o.device_loop_blocks > 0 && !resume && o.max_iterations_per_node <= 1 && !o.checkpoint_path &&
+                          !o.stop_after_steps && !o.progress;
+        lane.admit(&r, loop);
+        if(loop) {
+            if(lane.run_device_loop(&r, o.device_loop_blocks)) {
+                steps = lane.loop_steps;
+            } else {
+                // the queue or a list outgrew the loop's room: prove on the host-driven loop from the start
+                lane.release(&r);
+                lane.admit(&r, false);
+            }
+        }
         const std::vector<Request*> active{&r};
         auto checkpoint = [&]() {
             ProofState ps;

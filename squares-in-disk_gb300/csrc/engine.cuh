@@ -616,14 +616,21 @@ __device__ __forceinline__ void level_child_block(const LevelArgs& a, const bool
 #define SID_LEVEL_MIN_BLOCKS 4      // resident 128-thread blocks per SM the plain-form level kernel is compiled for
 #endif
 
-template<class L, class T, int MODE> __global__ void __launch_bounds__(128, SID_LEVEL_MIN_BLOCKS) k_level(const LevelArgs a) {
+/// The children of one block of 128 (block `vb` of the level): split, propagate, test rows, output, count. All
+/// 128 threads of the executing block call it. k_level runs block blockIdx.x; the device proof loop runs every
+/// block of the level on its persistent grid.
+template<class L, class T, int MODE> __device__ __forceinline__ void level_vblock(const LevelArgs& a, std::uint64_t vb) {
     const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
-    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::uint64_t t = vb * 128u + threadIdx.x;
     const bool valid = t < total;
     std::uint64_t q = 0;
     int c = 0;
     if(valid) split_index(t, a.nsub, q, c);
     level_child_block<L, T, MODE, true>(a, valid, a.in_begin + q, c, a.float_rows);
+}
+
+template<class L, class T, int MODE> __global__ void __launch_bounds__(128, SID_LEVEL_MIN_BLOCKS) k_level(const LevelArgs a) {
+    level_vblock<L, T, MODE>(a, blockIdx.x);
 }
 
 /// Float box of child c of a parent from its k_parent_f32 data: it contains the double child box of
@@ -682,9 +689,10 @@ __device__ __forceinline__ void filter_result_block(const LevelArgs& a, bool val
     }
 }
 
-template<class L> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) k_filter_f32(const LevelArgs a) {
+/// Float pass over block `vb` of a chunk's children (all 128 threads of the executing block call it).
+template<class L> __device__ __forceinline__ void filter_f32_vblock(const LevelArgs& a, std::uint64_t vb) {
     constexpr int N = L::NARGS;
-    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::uint64_t t = vb * 128u + threadIdx.x;
     const bool valid = t < a.n_child;
     bool ok = false;
     std::uint32_t tag = 0;
@@ -707,6 +715,10 @@ template<class L> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) 
         tag = item_tag(a, item);
     }
     filter_result_block(a, valid, tag, t, ok);
+}
+
+template<class L> __global__ void __launch_bounds__(128, SID_FILTER_MIN_BLOCKS) k_filter_f32(const LevelArgs a) {
+    filter_f32_vblock<L>(a, blockIdx.x);
 }
 
 constexpr std::uint64_t kParentRefuted = 1ull << 63;
@@ -768,8 +780,8 @@ template<class L, class H> __global__ void __launch_bounds__(128, SID_FILTER_MIN
 #define SID_ESC_MIN_BLOCKS 4        // resident 128-thread blocks per SM the double pass is compiled for (128 registers)
 #endif
 
-template<class L, int MODE> __global__ void __launch_bounds__(128, SID_ESC_MIN_BLOCKS) k_level_esc(const LevelArgs a) {
-    const std::uint64_t n = *a.esc_count;
+template<class L, int MODE> __device__ __forceinline__ void level_esc_grid(const LevelArgs& a) {
+    const std::uint64_t n = *reinterpret_cast<volatile unsigned long long*>(a.esc_count);
     const std::uint64_t stride = std::uint64_t(gridDim.x) * blockDim.x;
     // warp-uniform rounds: every lane of a warp takes part in each of its warp's rounds
     for(std::uint64_t base = std::uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
@@ -785,6 +797,10 @@ template<class L, int MODE> __global__ void __launch_bounds__(128, SID_ESC_MIN_B
         }
         level_child_block<L, double, MODE, false>(a, valid, item, c, true);
     }
+}
+
+template<class L, int MODE> __global__ void __launch_bounds__(128, SID_ESC_MIN_BLOCKS) k_level_esc(const LevelArgs a) {
+    level_esc_grid<L, MODE>(a);
 }
 
 /// Initial runtime box: compile-time bounds (fixed point / 1e6, rounded outward) tightened by 50*nargs
@@ -1183,6 +1199,9 @@ struct LemmaKernels {
     int n_operands;                   // expressions compared by the constraints (L::NOPERANDS)
     cudaError_t (*eval_operands)(int use_float, const double* lo, const double* hi, std::uint64_t n, std::uint64_t stride,
                                  double2* out, std::int8_t* und, cudaStream_t s);
+    // the device proof loop (proof_loop.cuh): cooperative launch, and its resident blocks per SM
+    cudaError_t (*proof_loop)(const struct LoopArgs& a, unsigned blocks, cudaStream_t s);
+    int (*proof_loop_occupancy)();
 };
 
 template<class L, class T> cudaError_t launch_level(int mode, const LevelArgs& a, cudaStream_t s) {

@@ -63,7 +63,8 @@ class SidProveOpts(ctypes.Structure):
                 ("progress_every_ms", ctypes.c_uint32), ("fp32_level_mask", ctypes.c_uint32),
                 ("checkpoint_path", ctypes.c_char_p), ("checkpoint_every_steps", ctypes.c_uint32),
                 ("stop_after_steps", ctypes.c_uint32), ("fp32_noprop_mask", ctypes.c_uint32),
-                ("part_index", ctypes.c_uint32), ("part_count", ctypes.c_uint32)]
+                ("part_index", ctypes.c_uint32), ("part_count", ctypes.c_uint32),
+                ("device_loop_blocks", ctypes.c_uint32)]
 
 
 class SidServerOpts(ctypes.Structure):
@@ -231,13 +232,14 @@ class Engine:
     def prove(self, lemma_id, generations=8, max_iterations=1, max_criticals=1 << 20, batch=0, precision=0,
               nargs=None, fetch=False, fp32_level_mask=0xFFFFFFFF, checkpoint=None, checkpoint_every=0, stop_after=0,
               resume_from=None, fp32_noprop_mask=None, part=None, progress=None, progress_first_ms=None,
-              progress_every_ms=None):
+              progress_every_ms=None, device_loop=0):
         """A whole proof (sid_prove), or its continuation from a checkpoint file (resume_from, sid_prove_resume).
         checkpoint/checkpoint_every/stop_after write checkpoints and stop early (result 'complete' False);
         fp32_noprop_mask: float-pass levels without propagation (None: the engine default, all levels);
         part = (index, count): prove one shard of the root partition (counts of all shards sum to the proof's);
         progress(dict): called between steps with queue_size, cuboids, leaves, criticals and queue_head (the
-        (lo, hi) pairs of one queued element, or None) after progress_first_ms, then every progress_every_ms."""
+        (lo, hi) pairs of one queued element, or None) after progress_first_ms, then every progress_every_ms;
+        device_loop > 0: the whole proof in one persistent kernel on that many blocks (sid_prove_opts)."""
         opts = SidProveOpts()
         self.L.sid_prove_opts_default(ctypes.byref(opts))
         opts.generation_count = generations
@@ -246,6 +248,7 @@ class Engine:
         opts.batch_elements = batch
         opts.precision = precision
         opts.fp32_level_mask = fp32_level_mask
+        opts.device_loop_blocks = device_loop
         if fp32_noprop_mask is not None:
             opts.fp32_noprop_mask = fp32_noprop_mask
         if part is not None:
