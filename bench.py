@@ -197,6 +197,7 @@ def prove_lemma_set(eng, sid, repeats=2):
                         "seconds": r["seconds"], "cuboids_per_s": r["cuboids"] / max(r["seconds"], 1e-9),
                         "escalated": r["escalated"], "step_elements": tune["step_elements"],
                         "fp32_level_mask": tune["fp32_level_mask"], "fp32_noprop_mask": tune["fp32_noprop_mask"],
+                        "device_loop_blocks": tune["loop_blocks"],
                         "level_escalation": tune["level_escalation"], "candidates": tune["candidates"]}
         tot["tuned_s"] = tot.get("tuned_s", 0.0) + r["seconds"]
         pub = published.get(name) or [None, None]

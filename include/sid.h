@@ -163,8 +163,9 @@ int sid_fetch_criticals(sid_engine* engine, int lemma_id, double* out, uint64_t 
  * float pass cannot refute / children); candidate configurations combine a threshold (levels whose rate
  * exceeds it skip the float pass and go straight to double) with a step size, and are timed by proving
  * the lemma, as long as max_seconds of proving allows. Every candidate must reproduce the first proof's
- * cuboid, leaf and critical counts or it is discarded. The fastest is stored with the lemma and used by
- * SID_PRECISION_FP32_TUNED proofs and servers. */
+ * cuboid, leaf and critical counts or it is discarded. Proofs shorter than 5 ms also try the device proof loop
+ * (sid_prove_opts.device_loop_blocks) on 38, 152 and 608 blocks. The fastest is stored with the lemma and used by
+ * SID_PRECISION_FP32_TUNED proofs and servers (servers drive their lanes from the host). */
 #define SID_MAX_LEVELS 16
 typedef struct sid_tuning {
     int64_t step_elements;                    /* queue elements per step */
@@ -177,6 +178,8 @@ typedef struct sid_tuning {
     double default_seconds;                   /* proof time with every level on the float pass, 65536 per step */
     uint32_t fp32_noprop_mask;                /* float-pass levels without propagation (sid_prove_opts; the
                                                  default all, or propagation on some levels if faster) */
+    uint32_t loop_blocks;                     /* > 0: tuned proofs run in the device proof loop on this many
+                                                 blocks (tried for proofs under 5 ms; sid_prove_opts) */
 } sid_tuning;
 
 int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid_tuning* out);

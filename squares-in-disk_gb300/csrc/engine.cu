@@ -1512,11 +1512,12 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
         bool first_done = false;
         // the device proof loop takes the whole proof (root partition included) when asked for and when the proof
         // needs nothing between steps from the host
-        const bool loop = o.device_loop_blocks > 0 && !resume && o.max_iterations_per_node <= 1 && !o.checkpoint_path &&
+        const unsigned loop_blocks = o.device_loop_blocks > 0 ? o.device_loop_blocks : (tuned ? lem->tuning.loop_blocks : 0u);
+        const bool loop = loop_blocks > 0 && !resume && o.max_iterations_per_node <= 1 && !o.checkpoint_path &&
                           !o.stop_after_steps && !o.progress;
         lane.admit(&r, loop);
         if(loop) {
-            if(lane.run_device_loop(&r, o.device_loop_blocks)) {
+            if(lane.run_device_loop(&r, loop_blocks)) {
                 steps = lane.loop_steps;
             } else {
                 // the queue or a list outgrew the loop's room: prove on the host-driven loop from the start
@@ -2079,6 +2080,8 @@ int sid_debug_inject_failure(int kind, int64_t countdown) {
     });
 }
 
+constexpr double kLoopTuneBelowSeconds = 0.005;   // proofs shorter than this also try the device proof loop
+
 int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid_tuning* out) {
     return guarded([&] {
         Lemma* l = get_lemma(engine, lemma_id);
@@ -2169,6 +2172,21 @@ int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid
                 if(same(r) && r.seconds < t.seconds) {
                     t.seconds = r.seconds;
                     t.step_elements = std::int64_t(step);
+                }
+            }
+            // the device proof loop, for proofs short enough that launches and host reads dominate
+            if(t.seconds < kLoopTuneBelowSeconds) {
+                for(unsigned blocks : {38u, 152u, 608u}) {
+                    if(spent > max_seconds) break;
+                    sid_result r{};
+                    o.device_loop_blocks = blocks;
+                    timed(std::uint64_t(t.step_elements), t.fp32_level_mask, r);
+                    o.device_loop_blocks = 0;
+                    ++t.candidates;
+                    if(same(r) && r.seconds < t.seconds) {
+                        t.seconds = r.seconds;
+                        t.loop_blocks = blocks;
+                    }
                 }
             }
         }

@@ -93,7 +93,8 @@ class SidTuning(ctypes.Structure):
     _fields_ = [("step_elements", ctypes.c_int64), ("fp32_level_mask", ctypes.c_uint32),
                 ("escalation_threshold", ctypes.c_float), ("levels", ctypes.c_int32), ("candidates", ctypes.c_uint32),
                 ("level_escalation", ctypes.c_double * MAX_LEVELS), ("seconds", ctypes.c_double),
-                ("default_seconds", ctypes.c_double), ("fp32_noprop_mask", ctypes.c_uint32)]
+                ("default_seconds", ctypes.c_double), ("fp32_noprop_mask", ctypes.c_uint32),
+                ("loop_blocks", ctypes.c_uint32)]
 
 
 class SidError(RuntimeError):
@@ -347,7 +348,8 @@ class Engine:
         return dict(step_elements=t.step_elements, fp32_level_mask=t.fp32_level_mask,
                     escalation_threshold=t.escalation_threshold, levels=t.levels, candidates=t.candidates,
                     level_escalation=[t.level_escalation[k] for k in range(min(t.levels, MAX_LEVELS))],
-                    seconds=t.seconds, default_seconds=t.default_seconds, fp32_noprop_mask=t.fp32_noprop_mask)
+                    seconds=t.seconds, default_seconds=t.default_seconds, fp32_noprop_mask=t.fp32_noprop_mask,
+                    loop_blocks=t.loop_blocks)
 
     def batch_profile(self, enable):
         """Record CUDA events around the ordering and evaluation kernels of the following batch calls."""

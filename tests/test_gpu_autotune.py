@@ -51,3 +51,18 @@ def test_tuned_configuration_is_used_by_a_server(engine):
         st = srv.wait(srv.submit(lid), 300000)
     assert (st["cuboids"], st["leaves"], st["escalated"]) == (direct["cuboids"], direct["leaves"], direct["escalated"])
     assert t["fp32_level_mask"] != 0
+
+
+@pytest.mark.parametrize("name", ["top_packing_1", "top_packing_2", "six_subcontainer"])
+def test_autotune_tries_the_device_loop_on_short_proofs(engine, name):
+    """Proofs under 5 ms also time the device proof loop; whichever form wins, a tuned proof keeps the published
+    counts, and a tuned served request (host-driven lanes) gives the same counts and escalations."""
+    lid = engine.register(sid.lemma_ir(name))
+    t = engine.autotune(lid, max_seconds=3.0)
+    assert t["default_seconds"] < 0.005 and t["candidates"] >= 4
+    assert t["loop_blocks"] in (0, 38, 152, 608)
+    r = engine.prove(lid, precision=sid.PRECISION_TUNED)
+    assert [r["cuboids"], r["leaves"]] == PUBLISHED[name] and r["criticals"] == 0
+    with sid.Server(engine, precision=sid.PRECISION_TUNED) as srv:
+        st = srv.wait(srv.submit(lid), 120000)
+    assert (st["cuboids"], st["leaves"], st["escalated"]) == (r["cuboids"], r["leaves"], r["escalated"])
