@@ -313,10 +313,29 @@ def batched_form(eng, sid, repeats=3):
                 best = (wall, res)
     wall, res = best
     cub = sum(r["cuboids"] for r in res)
-    return {"lemmas": list(BATCHED_LEMMAS), "wall_s": wall, "cuboids": cub, "cuboids_per_s": cub / wall,
-            "all_proved": all(r["proved"] for r in res),
-            "counts": {n: [r["cuboids"], r["leaves"]] for n, r in zip(BATCHED_LEMMAS, res)},
-            "escalated": {n: r["escalated"] for n, r in zip(BATCHED_LEMMAS, res)}}
+    out = {"lemmas": list(BATCHED_LEMMAS), "wall_s": wall, "cuboids": cub, "cuboids_per_s": cub / wall,
+           "all_proved": all(r["proved"] for r in res),
+           "counts": {n: [r["cuboids"], r["leaves"]] for n, r in zip(BATCHED_LEMMAS, res)},
+           "escalated": {n: r["escalated"] for n, r in zip(BATCHED_LEMMAS, res)}}
+    # the same four proofs in one persistent kernel over all of them (sid_prove_bundle): device time of the
+    # whole bundle, best of `repeats`, per grid size tried
+    with open(PUBLISHED) as f:
+        published = json.load(f)
+    bundle = {}
+    for blocks in (152, 304, 608, 0):
+        for precision, key in ((PRECISION_TUNED, "tuned"), (sid.PRECISION_FP32, "fp32")):
+            runs = [eng.prove_bundle(lids, precision=precision, blocks=blocks) for _ in range(repeats)]
+            r = min(runs, key=lambda x: x[0]["seconds"])
+            secs = r[0]["seconds"]
+            bundle["%s_blocks%d" % (key, blocks)] = {
+                "seconds": secs, "cuboids_per_s": sum(x["cuboids"] for x in r) / secs,
+                "counts_match_published": all([x["cuboids"], x["leaves"]] == published[n]
+                                              for n, x in zip(BATCHED_LEMMAS, r))}
+    best_key = min(bundle, key=lambda k: bundle[k]["seconds"])
+    out["one_kernel"] = {"kernel": "k_proof_loop_bundle (one cooperative persistent kernel over the four proofs)",
+                         "best": best_key, "seconds": bundle[best_key]["seconds"],
+                         "cuboids_per_s": bundle[best_key]["cuboids_per_s"], "runs": bundle}
+    return out
 
 
 def run_reference(args):

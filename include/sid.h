@@ -153,6 +153,21 @@ int sid_prove(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, sid_
 int sid_prove_resume(sid_engine* engine, int lemma_id, const sid_prove_opts* opts, const char* checkpoint_path,
                      sid_result* result);
 
+/* Whole proofs of several lemmas at once in one persistent kernel (no counterpart in the reference, whose
+ * driver proves one lemma per run_prover call; each proof is ProofDriver::run, proof_driver.hpp:472-489).
+ * lemma_ids: n (1 to 4) distinct registered double lemmas for which the build generated a bundle kernel
+ * (a line of a bundles.txt beside their IR; SID_ERR_NOT_COMPILED otherwise). The root partitions run one
+ * after the other over the whole grid; then every step takes up to opts->batch_elements elements (each
+ * lemma's default or tuned step otherwise) from the top of each proof's frontier, and the grid drains
+ * them all together, elements of different lemmas and depths side by side, each child returning to its
+ * own proof's frontier. results[j] is lemma_ids[j]'s proof with exactly the counts and criticals of
+ * sid_prove alone (sid_fetch_criticals per lemma afterwards); seconds is the whole bundle's time.
+ * opts: generation_count, precision (per lemma, as sid_prove), batch_elements, max_criticals_kept,
+ * fp32 masks, device_loop_blocks (grid size; 0: every block that can be resident). Re-iteration,
+ * checkpoints, progress and parts: SID_ERR_UNSUPPORTED. A proof whose frontier outgrows the loop's room
+ * is proved again by the host-driven loop. */
+int sid_prove_bundle(sid_engine* engine, int n, const int* lemma_ids, const sid_prove_opts* opts, sid_result* results);
+
 /* Copy the criticals retained by the last sid_prove of this lemma: n*2*nargs doubles, per critical
  * the (lo,hi) pairs of all variables (the on_critical calls of cpu_prover_core.hpp:137-149). */
 int sid_fetch_criticals(sid_engine* engine, int lemma_id, double* out, uint64_t capacity, uint64_t* n_out);

@@ -63,25 +63,45 @@ def build(ir_files=None, extra_ir_dirs=(), verbose=False, jobs=None):
     import codegen  # noqa: E402
 
     usable = list(ir_files)
-    subprocess.run([sys.executable, os.path.join(CSRC, "codegen.py"), "--out", GEN, *usable], check=True,
+    # bundles (several lemmas proved by one persistent kernel): bundles.txt beside the IR files
+    bundle_files = sorted({os.path.join(os.path.dirname(p), "bundles.txt") for p in usable} |
+                          {os.path.join(d, "bundles.txt") for d in extra_ir_dirs})
+    bundle_files = [b for b in bundle_files if os.path.exists(b)]
+    bundle_args = [x for b in bundle_files for x in ("--bundles", b)]
+    subprocess.run([sys.executable, os.path.join(CSRC, "codegen.py"), "--out", GEN, *bundle_args, *usable], check=True,
                    stdout=subprocess.DEVNULL if not verbose else None)
     gen_units = sorted(glob.glob(os.path.join(GEN, "lemma_*.cu")))
     wanted = {os.path.join(GEN, "lemma_" + _ns(p) + ".cu") for p in usable}
     for stale in set(gen_units) - wanted:
         os.remove(stale)
     gen_units = sorted(wanted)
-    units = gen_units + [os.path.join(GEN, "registry.cu"), os.path.join(CSRC, "engine.cu"),
-                         os.path.join(CSRC, "noalloc.cu")]
+    wanted_bundles = {os.path.join(GEN, "bundle_%s.cu" % name) for b in bundle_files for name, _ in codegen.read_bundles(b)}
+    for stale in set(glob.glob(os.path.join(GEN, "bundle_*.cu"))) - wanted_bundles:
+        os.remove(stale)
+    # separate compilation (-rdc) for the bundle units and the lemma units they call into, which export their
+    # proof-loop parts; a device-link step resolves those calls. Their registers are capped like the one-proof
+    # loop kernel's, so the bundle kernel keeps its residency.
+    parts = {os.path.join(GEN, "bpart_lemma_" + _ns(x) + ".cu") for b in bundle_files for _, slugs in codegen.read_bundles(b)
+             for x in slugs}
+    for stale in set(glob.glob(os.path.join(GEN, "bpart_*.cu"))) - parts:
+        os.remove(stale)
+    part_deps = {p: [os.path.join(GEN, os.path.basename(p)[len("bpart_"):])] for p in parts}
+    unit_flags = {u: ["-rdc=true"] for u in wanted_bundles}
+    unit_flags.update({u: ["-rdc=true", "-maxrregcount=128"] for u in parts})
+    units = sorted(parts) + gen_units + sorted(wanted_bundles) + [os.path.join(GEN, "registry.cu"),
+                                                                  os.path.join(CSRC, "engine.cu"),
+                                                                  os.path.join(CSRC, "noalloc.cu")]
     headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.hpp")) +
                      [os.path.join(REPO, "include", "sid.h")])
 
     def compile_unit(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         stamp_file = obj + ".stamp"
-        stamp = _stamp([src] + headers, NVCC_FLAGS)
+        flags = NVCC_FLAGS + unit_flags.get(src, [])
+        stamp = _stamp([src] + part_deps.get(src, []) + headers, flags)
         if os.path.exists(obj) and os.path.exists(stamp_file) and open(stamp_file).read() == stamp:
             return obj
-        cmd = [nvcc(), *NVCC_FLAGS, "-c", src, "-o", obj]
+        cmd = [nvcc(), *flags, "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -93,6 +113,19 @@ def build(ir_files=None, extra_ir_dirs=(), verbose=False, jobs=None):
 
     with ThreadPoolExecutor(max_workers=jobs or max(2, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_unit, units))
+    rdc_objs = [o for u, o in zip(units, objs) if u in unit_flags]
+    if rdc_objs:
+        dlink = os.path.join(BUILD, "device_link.o")
+        dlink_stamp = _stamp(rdc_objs, ["dlink"])
+        if not (os.path.exists(dlink) and os.path.exists(dlink + ".stamp") and open(dlink + ".stamp").read() == dlink_stamp):
+            cmd = [nvcc(), "-dlink", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC", *rdc_objs,
+                   "-o", dlink]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("device link failed:\n%s\n%s" % (r.stdout, r.stderr))
+            with open(dlink + ".stamp", "w") as f:
+                f.write(dlink_stamp)
+        objs = objs + [dlink]
     link_stamp = _stamp(objs, ["link"])
     lib_stamp = LIB + ".stamp"
     if not (os.path.exists(LIB) and os.path.exists(lib_stamp) and open(lib_stamp).read() == link_stamp):

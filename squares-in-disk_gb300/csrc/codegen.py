@@ -88,6 +88,9 @@ class Lemma:
         return any(n.op == op for n in self.nodes)
 
 
+BUNDLE_MAX = 4   # lemmas per bundle (kBundleMax of proof_loop.cuh)
+
+
 def fingerprint(text):
     """FNV-1a over the IR lines except the name line (same as lemma_ir.hpp)."""
     h = 1469598103934665603
@@ -672,6 +675,7 @@ def generate(lemma):
             plan = hoist_plan(L, var, r0, r1)
             if plan is not None:
                 hoisted.append((level, emit_hoisted(L, level, var, plan, w)))
+        w("#ifndef SID_LEMMA_DEFS_ONLY   // host launchers and launch table (a bundle part includes only the definitions)")
         w("static int hoist_values(int lv) {")
         w("    switch(lv) {")
         for level, nval in hoisted:
@@ -695,6 +699,8 @@ def generate(lemma):
         w("    }")
         w("}")
         w("")
+    if L.numtype == "f32":
+        w("#ifndef SID_LEMMA_DEFS_ONLY   // host launchers and launch table (a bundle part includes only the definitions)")
     w("static cudaError_t level(int mode, const LevelArgs& a, cudaStream_t s) { return launch_level<L, %s>(mode, a, s); }" % T_plain)
     w("static cudaError_t root_box(double2* o, cudaStream_t s) { return launch_root_box<L, %s>(o, s); }" % T_plain)
     w("static cudaError_t eval_batch(const BatchArgs& a, cudaStream_t s) { return launch_eval_batch<L, %s>(a, s); }" % T_plain)
@@ -714,9 +720,11 @@ def generate(lemma):
         w("static cudaError_t level_esc(int mode, const LevelArgs& a, unsigned blocks, cudaStream_t s) {")
         w("    return launch_level_esc<L>(mode, a, blocks, s);")
         w("}")
+    w("#endif")
     w("")
     w("} // namespace %s" % ns)
     w("")
+    w("#ifndef SID_LEMMA_DEFS_ONLY")
     w("extern const LemmaKernels kernels_%s;" % ns)
     prec = ("nullptr, nullptr, nullptr, nullptr, nullptr" if L.numtype == "f32" else
             "&{0}::filter_f32, &{0}::level_esc, &{0}::hoist_values, &{0}::prelude_f32, &{0}::filter_hoisted".format(ns))
@@ -724,28 +732,115 @@ def generate(lemma):
         ns, L.slug, L.fingerprint, L.nargs, len(L.bounds), "true" if L.numtype == "f32" else "false", ns, ns, ns, prec))
     w("    &%s::eval_batch_plain, %d, &%s::eval_operands, &%s::proof_loop, &%s::proof_loop_occupancy};" % (
         ns, len(operands), ns, ns, ns))
+    w("#endif")
     w("")
     w("} // namespace sid")
     return ns, "\n".join(out) + "\n"
 
 
+def read_bundles(path):
+    """Bundle specifications of a bundles file: one `name: lemma lemma ...` per line (# comments)."""
+    out = []
+    for line in open(path):
+        line = line.split("#", 1)[0].strip()
+        if not line:
+            continue
+        name, _, rest = line.partition(":")
+        slugs = rest.split()
+        if not re.fullmatch(r"[A-Za-z0-9_]+", name.strip()) or not 1 <= len(slugs) <= BUNDLE_MAX:
+            raise ValueError("%s: bad bundle line %r" % (path, line))
+        out.append((name.strip(), slugs))
+    return out
+
+
+def generate_bundle_part(lemma):
+    """The proof-loop parts of one lemma that bundle kernels call, in a unit of their own built with separate
+    compilation: the lemma unit's definitions (without its host launchers and launch table) and two exported
+    device functions, its root partition and its element processing."""
+    ns = "lemma_" + re.sub(r"[^A-Za-z0-9_]", "_", lemma.slug)
+    return "\n".join([
+        "// Generated by csrc/codegen.py -- do not edit.",
+        "// The proof-loop parts of %s that bundle kernels call (separate compilation)." % lemma.slug,
+        "#define SID_LEMMA_DEFS_ONLY",
+        '#include "%s.cu"' % ns,
+        "",
+        "namespace sid {",
+        "namespace %s {" % ns,
+        "__device__ bool loop_root(const LoopArgs& la, unsigned& gen) { return grid_root_partition<L, double>(la, gen); }",
+        "__device__ void loop_element(const LoopArgs& la, std::uint64_t e) { block_element<L, double>(la, e); }",
+        "} // namespace %s" % ns,
+        "} // namespace sid", ""])
+
+
+def generate_bundle(name, lemmas):
+    """A translation unit holding one persistent kernel over the listed lemmas (proof_loop.cuh's bundle loop),
+    instantiated with the lemmas in list order. Each lemma's root partition and element processing are the
+    loop_root/loop_element functions of its bundle part (generate_bundle_part), linked by the device-link step,
+    so this unit compiles in seconds."""
+    for L in lemmas:
+        if L.numtype == "f32":
+            raise ValueError("bundle %s: %s is a float lemma; bundles hold double lemmas" % (name, L.slug))
+    nss = ["lemma_" + re.sub(r"[^A-Za-z0-9_]", "_", L.slug) for L in lemmas]
+    types = ", ".join("%s::M" % ns for ns in nss)
+    out = ["// Generated by csrc/codegen.py -- do not edit.",
+           "// Bundle %s: %s proved together by one persistent kernel." % (name, ", ".join(L.slug for L in lemmas)),
+           '#include "engine.cuh"', '#include "proof_loop.cuh"', "", "namespace sid {"]
+    for ns in nss:
+        out += ["namespace %s {" % ns,
+                "__device__ bool loop_root(const LoopArgs& la, unsigned& gen);",
+                "__device__ void loop_element(const LoopArgs& la, std::uint64_t e);",
+                "struct M {",
+                "    __device__ static bool root(const LoopArgs& la, unsigned& gen) { return loop_root(la, gen); }",
+                "    __device__ static void element(const LoopArgs& la, std::uint64_t e) { loop_element(la, e); }",
+                "};",
+                "} // namespace %s" % ns]
+    out += ["static cudaError_t bundle_launch_%s(const BundleArgs& b, unsigned blocks, cudaStream_t s) {" % name,
+            "    return launch_proof_loop_bundle<%s>(b, blocks, s);" % types,
+            "}",
+            "static int bundle_occupancy_%s() { return proof_loop_bundle_occupancy<%s>(); }" % (name, types),
+            "extern const BundleKernels bundle_%s;" % name,
+            "const BundleKernels bundle_%s = {\"%s\", %d, {%s}, &bundle_launch_%s, &bundle_occupancy_%s};" % (
+                name, name, len(lemmas), ", ".join("0x%016xull" % L.fingerprint for L in lemmas), name, name),
+            "} // namespace sid"]
+    return "\n".join(out) + "\n"
+
+
+def write_if_changed(dest, code):
+    old = open(dest).read() if os.path.exists(dest) else None
+    if old != code:
+        with open(dest, "w") as f:
+            f.write(code)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
+    ap.add_argument("--bundles", action="append", default=[], help="bundles file (name: lemma lemma ...)")
     ap.add_argument("irs", nargs="+")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     names = []
+    by_slug = {}
     for p in args.irs:
         lemma = Lemma(p)
         ns, code = generate(lemma)
-        dest = os.path.join(args.out, ns + ".cu")
-        old = open(dest).read() if os.path.exists(dest) else None
-        if old != code:
-            with open(dest, "w") as f:
-                f.write(code)
+        write_if_changed(os.path.join(args.out, ns + ".cu"), code)
         names.append(ns)
-    reg = ["// Generated by csrc/codegen.py -- do not edit.", '#include "engine.cuh"', "", "namespace sid {"]
+        by_slug[lemma.slug] = lemma
+    bundles = []
+    for bf in args.bundles:
+        for name, slugs in read_bundles(bf):
+            missing = [x for x in slugs if x not in by_slug]
+            if missing:
+                raise ValueError("bundle %s names lemmas without IR: %s" % (name, ", ".join(missing)))
+            write_if_changed(os.path.join(args.out, "bundle_%s.cu" % name),
+                             generate_bundle(name, [by_slug[x] for x in slugs]))
+            for x in slugs:
+                ns = "lemma_" + re.sub(r"[^A-Za-z0-9_]", "_", x)
+                write_if_changed(os.path.join(args.out, "bpart_%s.cu" % ns), generate_bundle_part(by_slug[x]))
+            bundles.append(name)
+    reg = ["// Generated by csrc/codegen.py -- do not edit.", '#include "engine.cuh"', '#include "proof_loop.cuh"', "",
+           "namespace sid {"]
     for ns in names:
         reg.append("extern const LemmaKernels kernels_%s;" % ns)
     reg.append("extern const LemmaKernels* const kAllLemmas[] = {")
@@ -753,15 +848,21 @@ def main():
         reg.append("    &kernels_%s," % ns)
     reg.append("};")
     reg.append("extern const int kNumLemmas = %d;" % len(names))
+    for b in bundles:
+        reg.append("extern const BundleKernels bundle_%s;" % b)
+    reg.append("extern const BundleKernels* const kAllBundles[] = {")
+    for b in bundles:
+        reg.append("    &bundle_%s," % b)
+    if not bundles:
+        reg.append("    nullptr,")
+    reg.append("};")
+    reg.append("extern const int kNumBundles = %d;" % len(bundles))
     reg.append("} // namespace sid")
-    code = "\n".join(reg) + "\n"
-    dest = os.path.join(args.out, "registry.cu")
-    old = open(dest).read() if os.path.exists(dest) else None
-    if old != code:
-        with open(dest, "w") as f:
-            f.write(code)
+    write_if_changed(os.path.join(args.out, "registry.cu"), "\n".join(reg) + "\n")
     for ns in names:
         print(os.path.join(args.out, ns + ".cu"))
+    for b in bundles:
+        print(os.path.join(args.out, "bundle_%s.cu" % b))
     return 0
 
 

@@ -46,6 +46,8 @@
 namespace sid {
 extern const LemmaKernels* const kAllLemmas[];
 extern const int kNumLemmas;
+extern const BundleKernels* const kAllBundles[];
+extern const int kNumBundles;
 }
 
 namespace {
@@ -775,17 +777,13 @@ struct Lane {
         return std::max<std::uint64_t>(64, std::min(want, kLoopQueueBytes / per));
     }
 
-    /// A whole-lemma request admitted with root_on_device (its queue is the lane's loop queue), proved entirely in
-    /// the device proof loop (proof_loop.cuh) on `blocks` co-resident blocks (clamped to the device's limit for the
-    /// kernel). Returns false if the queue or a list would have overflowed (the request's counts are then
-    /// incomplete; the caller redoes the proof on the host-driven loop); throws SID_ERR_TIMEOUT if a barrier gave up.
-    bool run_device_loop(Request* r, unsigned blocks) {
+    /// Loop arguments for a whole-lemma request admitted with root_on_device (its queue is the lane's loop queue), on a
+    /// grid of G blocks: the root partition's lists and the per-block scratch sized for G, control words zeroed on the
+    /// lane's stream. la.sync is this lane's own control word (a bundle points it to its shared one).
+    void prepare_loop(Request* r, unsigned G, LoopArgs& la) {
         const int D = int(dyn.size()), S = int(stat.size());
         if(D < 1 || D > kLoopMaxLevels || S > kLoopMaxLevels) fail(SID_ERR_UNSUPPORTED, "device loop: too many levels");
-        const int occ = lem->k->proof_loop_occupancy ? lem->k->proof_loop_occupancy() : 0;
-        if(occ <= 0) fail(SID_ERR_UNSUPPORTED, "device loop: the kernel cannot be resident");
-        const unsigned G = std::max(1u, std::min(blocks, unsigned(occ) * unsigned(std::max(sm_count, 1))));
-        LoopArgs la{};
+        la = LoopArgs{};
         la.req = req_dev.p;
         la.tag = std::uint32_t(r->slot);
         la.nargs = n;
@@ -852,19 +850,38 @@ struct Lane {
         loop_ctl.reserve(1);
         cuda_check(cudaMemsetAsync(loop_ctl.p, 0, sizeof(LoopCtl), st), "loop control");
         la.ctl = loop_ctl.p;
-        launch_gate("device proof loop");
-        cuda_check(lem->k->proof_loop(la, G, st), "device proof loop launch");
+        la.sync = loop_ctl.p;
+    }
+
+    /// After a loop kernel: this proof's control words and counters, read back on the lane's stream (which the
+    /// kernel ran on, or which waits for it). Returns false if the proof's queue or a list would have overflowed
+    /// (its counts are then incomplete; the caller redoes the proof on the host-driven loop).
+    bool finish_loop(Request* r) {
         LoopCtl c{};
         ReqDev h{};
         cuda_check(cudaMemcpyAsync(&c, loop_ctl.p, sizeof(LoopCtl), cudaMemcpyDeviceToHost, st), "loop control");
         cuda_check(cudaMemcpyAsync(&h, req_dev.p + r->slot, sizeof(ReqDev), cudaMemcpyDeviceToHost, st), "request");
         cuda_check(cudaStreamSynchronize(st), "device proof loop");
         if(c.error == kLoopTimeout) fail(SID_ERR_TIMEOUT, "device proof loop: a grid barrier gave up");
-        // an append that did not fit is counted, not written; the proof is then redone on the host
-        if(c.error != kLoopOk || h.cnt[RC_OVERFLOW] != 0 || h.cnt[RC_QSIZE] != 0) return false;
+        // an append that did not fit is counted, not written
+        if(c.error != kLoopOk || c.overflow != 0 || h.cnt[RC_OVERFLOW] != 0 || h.cnt[RC_QSIZE] != 0) return false;
         std::memcpy(req_host[std::size_t(r->slot)].cnt, h.cnt, sizeof(h.cnt));
         loop_steps = std::uint32_t(c.steps);
         return true;
+    }
+
+    /// A whole-lemma request admitted with root_on_device, proved entirely in the device proof loop
+    /// (proof_loop.cuh) on `blocks` co-resident blocks (clamped to the device's limit for the kernel). Returns false
+    /// if the queue or a list would have overflowed; throws SID_ERR_TIMEOUT if a barrier gave up.
+    bool run_device_loop(Request* r, unsigned blocks) {
+        const int occ = lem->k->proof_loop_occupancy ? lem->k->proof_loop_occupancy() : 0;
+        if(occ <= 0) fail(SID_ERR_UNSUPPORTED, "device loop: the kernel cannot be resident");
+        const unsigned G = std::max(1u, std::min(blocks, unsigned(occ) * unsigned(std::max(sm_count, 1))));
+        LoopArgs la;
+        prepare_loop(r, G, la);
+        launch_gate("device proof loop");
+        cuda_check(lem->k->proof_loop(la, G, st), "device proof loop launch");
+        return finish_loop(r);
     }
     std::uint32_t loop_steps = 0;
 
@@ -963,6 +980,7 @@ struct Lane {
             LevelArgs a = a0;
             a.count_cuboids = true;
             a.float_rows = fp32_first;   // precision form, level without the float pass: float-first rows
+            a.lane_shift = lane_shift_for(total, std::uint64_t(std::max(sm_count, 1)) * 128u);
             cuda_check(lem->k->level(mode, a, st), "level kernel launch");
             return;
         }
@@ -1602,6 +1620,114 @@ void prove_one(sid_engine* eng, int lemma_id, const sid_prove_opts& o, sid_resul
     lem->criticals = std::move(r.criticals);
 }
 
+/// Configure the cached sid_prove lane of a lemma for a whole proof with options `o` (as prove_one does).
+Lane& prove_lane(sid_engine* eng, int lemma_id, const sid_prove_opts& o) {
+    Lemma* lem = get_lemma(eng, lemma_id);
+    auto& slot = eng->prove_lanes[lemma_id];
+    if(!slot) slot.reset(new Lane(eng, lem, eng->stream, false, eng->sm_count, 1));
+    Lane& lane = *slot;
+    const bool tuned = o.precision == SID_PRECISION_FP32_TUNED && lem->tuned;
+    const std::uint64_t step = o.batch_elements > 0 ? std::uint64_t(o.batch_elements)
+                                                    : (tuned ? std::uint64_t(lem->tuning.step_elements) : kDefaultStep);
+    lane.configure(step, o.precision != SID_PRECISION_PLAIN, tuned ? lem->tuning.fp32_level_mask : o.fp32_level_mask,
+                   tuned ? lem->tuning.fp32_noprop_mask : o.fp32_noprop_mask);
+    lane.set_iteration(o.max_iterations_per_node, o.iteration_volume_criterion, o.iteration_single_dimension_criterion);
+    return lane;
+}
+
+/// Whole proofs of several lemmas in one bundle kernel (sid_prove_bundle): the caller's j-th lemma is proof pos[j]
+/// of the compiled bundle `bk`. Each proof is one request on its lemma's cached lane, admitted with its root on the
+/// device; all these lanes run on the engine's stream, which the bundle kernel runs on too. A proof whose queue or
+/// lists outgrew the loop's room is proved again on its host-driven lane, as sid_prove does.
+void prove_bundle(sid_engine* eng, const BundleKernels* bk, const std::vector<int>& ids, const std::vector<int>& pos,
+                  const sid_prove_opts& o, sid_result* res) {
+    const std::size_t n = ids.size();
+    std::vector<Lane*> lanes(n);
+    std::vector<Request> reqs(n);
+    for(std::size_t j = 0; j < n; ++j) {
+        lanes[j] = &prove_lane(eng, ids[j], o);
+        Request& r = reqs[j];
+        r.lem = get_lemma(eng, ids[j]);
+        r.lemma_id = ids[j];
+        r.full = true;
+        r.generations = o.generation_count;
+        r.crit_cap = o.max_criticals_kept;
+    }
+    const int occ = bk->occupancy();
+    if(occ <= 0) fail(SID_ERR_UNSUPPORTED, "bundle %s: the kernel cannot be resident", bk->name);
+    const unsigned most = unsigned(occ) * unsigned(std::max(eng->sm_count, 1));
+    const unsigned G = o.device_loop_blocks > 0 ? std::max(1u, std::min(o.device_loop_blocks, most)) : most;
+    cudaEvent_t ev0, ev1;
+    cuda_check(cudaEventCreate(&ev0), "event");
+    cuda_check(cudaEventCreate(&ev1), "event");
+    std::vector<std::uint32_t> steps(n, 0);
+    auto release_all = [&] {
+        for(std::size_t j = 0; j < n; ++j) {
+            try { lanes[j]->release(&reqs[j]); } catch(...) {}
+        }
+    };
+    try {
+        cuda_check(cudaEventRecord(ev0, eng->stream), "event record");
+        BundleArgs b{};
+        b.n = int(n);
+        for(std::size_t j = 0; j < n; ++j) {
+            lanes[j]->admit(&reqs[j], true);
+            lanes[j]->prepare_loop(&reqs[j], G, b.p[pos[j]]);
+        }
+        LoopCtl* sync = b.p[0].ctl;
+        for(std::size_t i = 0; i < n; ++i) b.p[i].sync = sync;
+        launch_gate("bundle proof loop");
+        cuda_check(bk->launch(b, G, eng->stream), "bundle proof loop launch");
+        LoopCtl c{};
+        cuda_check(cudaMemcpyAsync(&c, sync, sizeof(LoopCtl), cudaMemcpyDeviceToHost, eng->stream), "bundle control");
+        cuda_check(cudaStreamSynchronize(eng->stream), "bundle proof loop");
+        if(c.error == kLoopTimeout) fail(SID_ERR_TIMEOUT, "bundle proof loop: a grid barrier gave up");
+        for(std::size_t j = 0; j < n; ++j) {
+            Lane& lane = *lanes[j];
+            Request& r = reqs[j];
+            if(lane.finish_loop(&r) && c.error == kLoopOk) {
+                steps[j] = lane.loop_steps;
+                continue;
+            }
+            // the loop stopped early: this proof again on the host-driven loop, from its root
+            lane.release(&r);
+            lane.admit(&r, false);
+            const std::vector<Request*> active{&r};
+            while(lane.queue_size(&r) > 0) {
+                lane.run_step(active);
+                ++steps[j];
+            }
+        }
+        cuda_check(cudaEventRecord(ev1, eng->stream), "event record");
+        cuda_check(cudaEventSynchronize(ev1), "event sync");
+        for(std::size_t j = 0; j < n; ++j) lanes[j]->fetch_criticals(&reqs[j]);
+    } catch(...) {
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        release_all();
+        throw;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    for(std::size_t j = 0; j < n; ++j) {
+        const ReqDev last = lanes[j]->counters_of(&reqs[j]);
+        lanes[j]->release(&reqs[j]);
+        sid_result* out = res + j;
+        out->num_cuboids = last.cnt[RC_CUBOIDS];
+        out->num_leaf_cuboids = last.cnt[RC_LEAVES];
+        out->num_critical_cuboids = last.cnt[RC_CRITICALS];
+        out->num_repeated_nodes = last.cnt[RC_REPEATED];
+        out->criticals_stored = std::min<std::uint64_t>(out->num_critical_cuboids, reqs[j].crit_cap);
+        out->escalated = last.cnt[RC_ESCALATED];
+        out->seconds = double(ms) / 1000.0;
+        out->complete = 1;
+        out->steps = steps[j];
+        reqs[j].lem->criticals = std::move(reqs[j].criticals);
+    }
+}
+
 } // namespace
 
 /// The served form: one worker thread, stream and lane per lemma.
@@ -1936,6 +2062,56 @@ int sid_prove_resume(sid_engine* engine, int lemma_id, const sid_prove_opts* opt
         set_device(engine);
         std::memset(result, 0, sizeof(*result));
         prove_one(engine, lemma_id, o, result, 0, nullptr, &ps);
+    });
+}
+
+int sid_prove_bundle(sid_engine* engine, int n, const int* lemma_ids, const sid_prove_opts* opts, sid_result* results) {
+    return guarded([&] {
+        if(!engine || !lemma_ids || !results) fail(SID_ERR_INVALID, "null argument");
+        if(n < 1 || n > kBundleMax) fail(SID_ERR_INVALID, "a bundle proves 1 to %d lemmas, not %d", kBundleMax, n);
+        sid_prove_opts o;
+        if(opts) o = *opts; else sid_prove_opts_default(&o);
+        check_precision(o.precision);
+        if(o.generation_count > 250) fail(SID_ERR_INVALID, "generation_count too large");
+        if(o.max_iterations_per_node > 1 || o.checkpoint_path || o.stop_after_steps || o.progress || o.part_count > 1) {
+            fail(SID_ERR_UNSUPPORTED, "bundled proofs take no node re-iteration, checkpoints, progress or parts");
+        }
+        std::vector<int> ids(lemma_ids, lemma_ids + n);
+        std::vector<std::uint64_t> fps;
+        for(int j = 0; j < n; ++j) {
+            Lemma* l = get_lemma(engine, ids[std::size_t(j)]);
+            if(l->k->is_f32) fail(SID_ERR_UNSUPPORTED, "bundles hold double lemmas; '%s' is a float lemma", l->ir.name.c_str());
+            for(int k = 0; k < j; ++k) {
+                if(ids[std::size_t(k)] == ids[std::size_t(j)]) fail(SID_ERR_INVALID, "lemma %d appears twice", ids[std::size_t(j)]);
+            }
+            fps.push_back(l->ir.fingerprint);
+        }
+        // the compiled bundle of exactly these lemmas, in any order
+        const BundleKernels* bk = nullptr;
+        std::vector<int> pos(std::size_t(n), -1);
+        for(int b = 0; b < kNumBundles && !bk; ++b) {
+            const BundleKernels* c = kAllBundles[b];
+            if(!c || c->n != n) continue;
+            std::vector<int> p(std::size_t(n), -1);
+            std::vector<bool> used(std::size_t(n), false);
+            bool all = true;
+            for(int j = 0; j < n && all; ++j) {
+                all = false;
+                for(int i = 0; i < n; ++i) {
+                    if(!used[std::size_t(i)] && c->fingerprints[i] == fps[std::size_t(j)]) {
+                        used[std::size_t(i)] = true;
+                        p[std::size_t(j)] = i;
+                        all = true;
+                        break;
+                    }
+                }
+            }
+            if(all) { bk = c; pos = p; }
+        }
+        if(!bk) fail(SID_ERR_NOT_COMPILED, "no bundle kernel was generated for these %d lemmas; list them in a bundles.txt", n);
+        set_device(engine);
+        std::memset(results, 0, sizeof(sid_result) * std::size_t(n));
+        prove_bundle(engine, bk, ids, pos, o, results);
     });
 }
 

@@ -318,7 +318,22 @@ struct LevelArgs {
     // values hval[k*pstride + j] and their flags hbits[j] (kParentRefuted: no child can satisfy the rows)
     const float2* hval;
     const std::uint64_t* hbits;
+    // dense levels: each child takes 1 << lane_shift lanes (one of them works), so that a small level's children
+    // are spread over more warps (lane_shift_for)
+    std::uint32_t lane_shift;
 };
+
+/// Lane shift of a dense level with `total` children on `threads` threads (one pass over the GPU's SM
+/// sub-partitions: SMs x 128): the largest shift up to 5 (one child per warp) with which the children still fit.
+/// GB300 runs a warp's FP64 instruction in its sub-partition's narrow FP64 unit for the same time however many
+/// of its lanes take part, so a level of fewer children than the GPU has lanes finishes sooner with fewer
+/// children per warp: each warp then executes only its own children's paths through the propagation
+/// instead of the union of 32 divergent ones, on otherwise idle sub-partitions.
+__host__ __device__ __forceinline__ std::uint32_t lane_shift_for(std::uint64_t total, std::uint64_t threads) {
+    std::uint32_t s = 0;
+    while(s < 5 && (total << (s + 1)) <= threads) ++s;
+    return s;
+}
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -621,8 +636,9 @@ __device__ __forceinline__ void level_child_block(const LevelArgs& a, const bool
 /// block of the level on its persistent grid.
 template<class L, class T, int MODE> __device__ __forceinline__ void level_vblock(const LevelArgs& a, std::uint64_t vb) {
     const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
-    const std::uint64_t t = vb * 128u + threadIdx.x;
-    const bool valid = t < total;
+    const std::uint64_t t0 = vb * 128u + threadIdx.x;
+    const std::uint64_t t = t0 >> a.lane_shift;
+    const bool valid = (t0 & ((std::uint64_t(1) << a.lane_shift) - 1u)) == 0 && t < total;
     std::uint64_t q = 0;
     int c = 0;
     if(valid) split_index(t, a.nsub, q, c);
@@ -1208,7 +1224,8 @@ template<class L, class T> cudaError_t launch_level(int mode, const LevelArgs& a
     const std::uint64_t total = a.n_in * std::uint64_t(a.nsub);
     if(total == 0) return cudaSuccess;
     const unsigned threads = 128;
-    const std::uint64_t blocks = (total + threads - 1) / threads;
+    if(a.lane_shift > 5) return cudaErrorInvalidValue;
+    const std::uint64_t blocks = ((total << a.lane_shift) + threads - 1) / threads;
     if(blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     switch(mode) {
         case MODE_EMIT: k_level<L, T, MODE_EMIT><<<unsigned(blocks), threads, 0, s>>>(a); break;

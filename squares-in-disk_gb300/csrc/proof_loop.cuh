@@ -78,7 +78,8 @@ struct LoopArgs {
     float2* b_pbox; float4* b_psplit; std::uint64_t b_p_cap;   // b_p_cap parents per block
     std::uint32_t* b_esc; std::uint64_t b_esc_cap;
     unsigned long long* b_ctl;             // kBlockCtlWords per block
-    LoopCtl* ctl;
+    LoopCtl* ctl;                          // this proof's counters (root partition lists, steps, list overflow)
+    LoopCtl* sync;                         // the grid barrier and error word: ctl itself, or a bundle's shared one
 };
 
 constexpr unsigned kLoopBarrierLimit = 1u << 22;   // polls (with a short sleep each) before a barrier gives up
@@ -427,13 +428,14 @@ template<class L, class T, int MODE> __device__ bool grid_level(const LoopArgs& 
     if(!fp32) {
         a.count_cuboids = true;
         a.float_rows = la.fp32;
-        const std::uint64_t nb = (total + 127) / 128;
+        a.lane_shift = lane_shift_for(total, std::uint64_t(gridDim.x) * blockDim.x);
+        const std::uint64_t nb = ((total << a.lane_shift) + 127) / 128;
         for(std::uint64_t vb = blockIdx.x; vb < nb; vb += gridDim.x) level_vblock<L, T, MODE>(a, vb);
         return true;
     }
     loop_parent_f32(a.in_box, a.in_stride, 0, a.n_in, L::NARGS, a.var, a.nsub, la.pbox, la.psplit,
                     std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x, std::uint64_t(gridDim.x) * blockDim.x);
-    if(!loop_barrier(la.ctl, gen)) return false;
+    if(!loop_barrier(la.sync, gen)) return false;
     a.count_cuboids = false;
     a.fp32_noprop = true;
     a.pbox = la.pbox;
@@ -449,9 +451,9 @@ template<class L, class T, int MODE> __device__ bool grid_level(const LoopArgs& 
         if(blockIdx.x == 0 && threadIdx.x == 0) la.ctl->esc[k ^ 1] = 0;   // the other chunk's counter is free
         const std::uint64_t nb = (a.n_child + 127) / 128;
         for(std::uint64_t vb = blockIdx.x; vb < nb; vb += gridDim.x) filter_f32_vblock<L>(a, vb);
-        if(!loop_barrier(la.ctl, gen)) return false;
+        if(!loop_barrier(la.sync, gen)) return false;
         if constexpr(sizeof(T) == sizeof(double)) level_esc_grid<L, MODE>(a);
-        if(!loop_barrier(la.ctl, gen)) return false;
+        if(!loop_barrier(la.sync, gen)) return false;
     }
     // every chunk's double pass has finished: both counters start the next float-pass level at zero (the
     // caller's barrier orders this before that level's float pass)
@@ -491,7 +493,7 @@ template<class L, class T> __device__ bool grid_root_partition(const LoopArgs& l
         if(last) {
             a.row_begin = n - 1;
             a.row_end = n;
-            return grid_level<L, T, MODE_QUEUE>(la, a, d, gen) && loop_barrier(la.ctl, gen);
+            return grid_level<L, T, MODE_QUEUE>(la, a, d, gen) && loop_barrier(la.sync, gen);
         }
         a.row_begin = a.row_end = 0;
         a.out_box = la.dl_box[d + 1];
@@ -501,10 +503,10 @@ template<class L, class T> __device__ bool grid_root_partition(const LoopArgs& l
         a.out_tag = la.dl_tag[d + 1];
         a.out_count = &la.ctl->dyn[d + 1];
         if(!grid_level<L, T, MODE_EMIT>(la, a, d, gen)) return false;
-        if(!loop_barrier(la.ctl, gen)) return false;
+        if(!loop_barrier(la.sync, gen)) return false;
         n_in = loop_read(&la.ctl->dyn[d + 1]);
         if(n_in > la.dl_cap[d + 1]) {
-            if(blockIdx.x == 0 && threadIdx.x == 0) loop_set_error(la.ctl, kLoopListOverflow);
+            if(blockIdx.x == 0 && threadIdx.x == 0) loop_set_error(la.sync, kLoopListOverflow);
             return false;
         }
         if(n_in == 0) return true;
@@ -531,7 +533,7 @@ template<class L, class T> __global__ void __launch_bounds__(128, SID_LOOP_MIN_B
         const std::uint64_t q = loop_read(&r->cnt[RC_QSIZE]);
         const bool q_over = loop_read(&r->cnt[RC_OVERFLOW]) != 0;
         if(q_over || *reinterpret_cast<volatile unsigned*>(&la.ctl->overflow) != 0u) {
-            if(blockIdx.x == 0 && threadIdx.x == 0) loop_set_error(la.ctl, q_over ? kLoopQueueOverflow : kLoopListOverflow);
+            if(blockIdx.x == 0 && threadIdx.x == 0) loop_set_error(la.sync, q_over ? kLoopQueueOverflow : kLoopListOverflow);
             return;
         }
         if(q == 0) break;
@@ -544,12 +546,12 @@ template<class L, class T> __global__ void __launch_bounds__(128, SID_LOOP_MIN_B
             la.step_tag[i] = la.tag;
         }
         if(blockIdx.x == 0 && threadIdx.x == 0) la.ctl->steps = step + 1;
-        if(!loop_barrier(la.ctl, gen)) return;
+        if(!loop_barrier(la.sync, gen)) return;
         // popped: children append from here (a queue append reserves its slot atomically from this size)
         if(blockIdx.x == 0 && threadIdx.x == 0) r->cnt[RC_QSIZE] = begin;
-        if(!loop_barrier(la.ctl, gen)) return;
+        if(!loop_barrier(la.sync, gen)) return;
         for(std::uint64_t e = blockIdx.x; e < take; e += gridDim.x) block_element<L, T>(la, e);
-        if(!loop_barrier(la.ctl, gen)) return;
+        if(!loop_barrier(la.sync, gen)) return;
     }
 }
 
@@ -565,5 +567,133 @@ template<class L, class T> int proof_loop_occupancy() {
     if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_proof_loop<L, T>, 128, 0) != cudaSuccess) return 0;
     return n;
 }
+
+// ---- Bundles: proofs of several lemmas in one persistent kernel over one grid.
+//
+// A bundle kernel is compiled for a fixed list of lemmas (csrc/codegen.py generates one per configured bundle);
+// proof i runs the generated code of the list's i-th lemma. The root partitions run one after the other over the
+// whole grid; then every step takes up to `step` elements from the top of each proof's frontier into that proof's
+// step list, and the whole grid drains the union of the step lists: block b takes items b, b + grid, ... of the
+// concatenation, whatever proof they belong to, so elements of different lemmas and depths are processed side by
+// side, and every child goes back to its own proof's frontier. Each proof keeps its own counters, frontier,
+// critical store and per-block scratch exactly as in the one-proof loop, so its counts are those of the proof
+// run alone. Every proof's `sync` is the bundle's one barrier and error word.
+
+constexpr int kBundleMax = 4;
+
+struct BundleArgs {
+    int n;                                 // proofs (at most kBundleMax; the kernel's lemma list has n entries)
+    LoopArgs p[kBundleMax];
+};
+static_assert(sizeof(BundleArgs) <= 32000, "bundle arguments must fit the kernel parameter space");
+
+// Each member type M of a bundle kernel gives its lemma's root partition and element processing as
+// M::root(la, gen) and M::element(la, e): grid_root_partition<L, double> and block_element<L, double> of the
+// lemma, compiled in the lemma's own translation unit with separate compilation (csrc/codegen.py), so the bundle
+// kernel's own unit stays small.
+template<int I, class L0, class... Ls> __device__ bool bundle_roots(const BundleArgs& b, unsigned& gen) {
+    if(I < b.n && !L0::root(b.p[I], gen)) return false;
+    if constexpr(sizeof...(Ls) > 0) {
+        return bundle_roots<I + 1, Ls...>(b, gen);
+    } else {
+        return true;
+    }
+}
+
+template<int I, class L0, class... Ls> __device__ void bundle_element(const BundleArgs& b, int i, std::uint64_t e) {
+    if(i == I) {
+        L0::element(b.p[I], e);
+    } else {
+        if constexpr(sizeof...(Ls) > 0) bundle_element<I + 1, Ls...>(b, i, e);
+    }
+}
+
+/// Copy `take` elements from position `begin` of a proof's frontier into its step list (grid-stride).
+__device__ __forceinline__ void loop_take(const LoopArgs& la, std::uint64_t begin, std::uint64_t take) {
+    const ReqDev* r = la.req + la.tag;
+    const std::uint64_t stride = std::uint64_t(gridDim.x) * blockDim.x;
+    for(std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < take; i += stride) {
+        for(int v = 0; v < la.nargs; ++v) {
+            la.step_box[std::uint64_t(v) * la.step_cap + i] = r->qbox[std::uint64_t(v) * r->qcap + begin + i];
+        }
+        la.step_depth[i] = r->qdepth[begin + i];
+        la.step_tag[i] = la.tag;
+    }
+}
+
+/// The bundle loop (launched cooperatively). Double lemmas only; the precision form per proof (LoopArgs::fp32).
+template<class... Ls> __global__ void __launch_bounds__(128, SID_LOOP_MIN_BLOCKS) k_proof_loop_bundle(const BundleArgs b) {
+    static_assert(sizeof...(Ls) >= 1 && sizeof...(Ls) <= kBundleMax, "a bundle holds 1 to kBundleMax lemmas");
+    unsigned gen = 0;
+    LoopCtl* sync = b.p[0].sync;
+    if(!bundle_roots<0, Ls...>(b, gen)) return;
+    for(std::uint64_t step = 0;; ++step) {
+        std::uint64_t first[kBundleMax + 1], begin[kBundleMax];
+        first[0] = 0;
+        bool q_over = false, l_over = false;
+        for(int i = 0; i < kBundleMax; ++i) {
+            std::uint64_t take = 0;
+            begin[i] = 0;
+            if(i < b.n) {
+                const LoopArgs& la = b.p[i];
+                const ReqDev* r = la.req + la.tag;
+                const std::uint64_t q = loop_read(&r->cnt[RC_QSIZE]);
+                q_over = q_over || loop_read(&r->cnt[RC_OVERFLOW]) != 0;
+                l_over = l_over || *reinterpret_cast<volatile unsigned*>(&la.ctl->overflow) != 0u;
+                if(step < la.max_steps) take = q < la.step ? q : la.step;
+                begin[i] = q - take;
+            }
+            first[i + 1] = first[i] + take;
+        }
+        if(q_over || l_over) {
+            if(blockIdx.x == 0 && threadIdx.x == 0) loop_set_error(sync, q_over ? kLoopQueueOverflow : kLoopListOverflow);
+            return;
+        }
+        const std::uint64_t total = first[kBundleMax];
+        if(total == 0) break;
+        for(int i = 0; i < b.n; ++i) {
+            const std::uint64_t take = first[i + 1] - first[i];
+            if(take == 0) continue;
+            loop_take(b.p[i], begin[i], take);
+            if(blockIdx.x == 0 && threadIdx.x == 0) b.p[i].ctl->steps = step + 1;
+        }
+        if(!loop_barrier(sync, gen)) return;
+        // popped: children append from here
+        if(blockIdx.x == 0 && threadIdx.x == 0) {
+            for(int i = 0; i < b.n; ++i) {
+                if(first[i + 1] > first[i]) b.p[i].req[b.p[i].tag].cnt[RC_QSIZE] = begin[i];
+            }
+        }
+        if(!loop_barrier(sync, gen)) return;
+        for(std::uint64_t g = blockIdx.x; g < total; g += gridDim.x) {
+            int i = 0;
+            while(g >= first[i + 1]) ++i;
+            bundle_element<0, Ls...>(b, i, g - first[i]);
+        }
+        if(!loop_barrier(sync, gen)) return;
+    }
+}
+
+template<class... Ls> cudaError_t launch_proof_loop_bundle(const BundleArgs& b, unsigned blocks, cudaStream_t s) {
+    if(b.n != int(sizeof...(Ls))) return cudaErrorInvalidValue;
+    void* params[] = {const_cast<BundleArgs*>(&b)};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_proof_loop_bundle<Ls...>), dim3(blocks), dim3(128),
+                                       params, 0, s);
+}
+
+template<class... Ls> int proof_loop_bundle_occupancy() {
+    int n = 0;
+    if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_proof_loop_bundle<Ls...>, 128, 0) != cudaSuccess) return 0;
+    return n;
+}
+
+/// Host-side table of one compiled bundle.
+struct BundleKernels {
+    const char* name;
+    int n;
+    std::uint64_t fingerprints[kBundleMax];   // of the lemma whose code proof i runs
+    cudaError_t (*launch)(const BundleArgs& b, unsigned blocks, cudaStream_t s);
+    int (*occupancy)();
+};
 
 } // namespace sid

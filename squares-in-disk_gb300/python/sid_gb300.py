@@ -25,7 +25,7 @@ EXPORTED = ["sid_prove_opts_default", "sid_last_error", "sid_engine_create", "si
             "sid_eval_batch", "sid_eval_batch_device", "sid_leaf_hull_noalloc", "sid_server_opts_default",
             "sid_server_create", "sid_server_destroy", "sid_submit", "sid_request_poll", "sid_request_wait",
             "sid_request_criticals", "sid_request_release", "sid_eval_batch_profile", "sid_eval_batch_profile_read",
-            "sid_lemma_autotune", "sid_prove_resume", "sid_lemma_batch_order", "sid_eval_batch_plain_device",
+            "sid_lemma_autotune", "sid_prove_resume", "sid_prove_bundle", "sid_lemma_batch_order", "sid_eval_batch_plain_device",
             "sid_lemma_operands", "sid_eval_operands_device", "sid_debug_inject_failure"]
 
 PRECISION_PLAIN, PRECISION_FP32, PRECISION_TUNED = 0, 1, 2
@@ -124,6 +124,8 @@ def load(path=LIB_PATH):
     L.sid_prove.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(SidProveOpts), ctypes.POINTER(SidResult)]
     L.sid_prove_resume.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(SidProveOpts), ctypes.c_char_p,
                                    ctypes.POINTER(SidResult)]
+    L.sid_prove_bundle.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                   ctypes.POINTER(SidProveOpts), ctypes.POINTER(SidResult)]
     L.sid_fetch_criticals.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
                                       ctypes.POINTER(ctypes.c_uint64)]
     L.sid_eval_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
@@ -290,6 +292,39 @@ class Engine:
                                               ctypes.byref(got)))
             out["boxes"] = buf[: got.value * 2 * nargs].reshape(-1, nargs, 2)
         return out
+
+    def prove_bundle(self, lemma_ids, generations=8, precision=0, batch=0, max_criticals=1 << 20, blocks=0,
+                     fp32_level_mask=0xFFFFFFFF, fp32_noprop_mask=None, nargs=None, fetch=False):
+        """Whole proofs of several lemmas in one persistent kernel (sid_prove_bundle); a list of result dicts in
+        the order of lemma_ids (with fetch and nargs, a list of n_vars per lemma: their critical boxes too)."""
+        n = len(lemma_ids)
+        opts = SidProveOpts()
+        self.L.sid_prove_opts_default(ctypes.byref(opts))
+        opts.generation_count = generations
+        opts.max_criticals_kept = max_criticals
+        opts.batch_elements = batch
+        opts.precision = precision
+        opts.fp32_level_mask = fp32_level_mask
+        opts.device_loop_blocks = blocks
+        if fp32_noprop_mask is not None:
+            opts.fp32_noprop_mask = fp32_noprop_mask
+        ids = (ctypes.c_int * n)(*lemma_ids)
+        res = (SidResult * n)()
+        _check(self.L.sid_prove_bundle(self.h, n, ids, ctypes.byref(opts), res))
+        outs = []
+        for j, r in enumerate(res):
+            out = dict(cuboids=r.num_cuboids, leaves=r.num_leaf_cuboids, criticals=r.num_critical_cuboids,
+                       repeated=r.num_repeated_nodes, stored=r.criticals_stored, escalated=r.escalated,
+                       seconds=r.seconds, complete=bool(r.complete), steps=r.steps)
+            if fetch and r.criticals_stored:
+                nv = nargs[j]
+                buf = np.zeros(r.criticals_stored * 2 * nv, dtype=np.float64)
+                got = ctypes.c_uint64()
+                _check(self.L.sid_fetch_criticals(self.h, lemma_ids[j], buf.ctypes.data, r.criticals_stored,
+                                                  ctypes.byref(got)))
+                out["boxes"] = buf[: got.value * 2 * nv].reshape(-1, nv, 2)
+            outs.append(out)
+        return outs
 
     def eval_batch(self, lemma_id, lo, hi):
         lo = np.ascontiguousarray(lo, dtype=np.float64)

@@ -103,7 +103,8 @@ def test_oracle_row_order_is_the_code_generators(oracle):
     sys.path.insert(0, os.path.join(REPO, "squares-in-disk_gb300", "csrc"))
     import codegen
     names = [(n, sid.lemma_ir(n)) for n in sid.lemma_names()]
-    names += [(f[:-6], open(os.path.join(sid.KAT_DIR, f)).read()) for f in sorted(os.listdir(sid.KAT_DIR))]
+    names += [(f[:-6], open(os.path.join(sid.KAT_DIR, f)).read()) for f in sorted(os.listdir(sid.KAT_DIR))
+              if f.endswith(".sidir")]
     for name, ir in names:
         with tempfile.NamedTemporaryFile("w", suffix=".sidir", delete=False) as f:
             f.write(ir)
