@@ -767,7 +767,9 @@ def generate_bundle_part(lemma):
         "namespace sid {",
         "namespace %s {" % ns,
         "__device__ bool loop_root(const LoopArgs& la, unsigned& gen) { return grid_root_partition<L, double>(la, gen); }",
-        "__device__ void loop_element(const LoopArgs& la, std::uint64_t e) { block_element<L, double>(la, e); }",
+        "__device__ void loop_elements(const LoopArgs& la, std::uint64_t e0, std::uint64_t k) {",
+        "    block_elements<L, double>(la, e0, k);",
+        "}",
         "} // namespace %s" % ns,
         "} // namespace sid", ""])
 
@@ -775,7 +777,7 @@ def generate_bundle_part(lemma):
 def generate_bundle(name, lemmas):
     """A translation unit holding one persistent kernel over the listed lemmas (proof_loop.cuh's bundle loop),
     instantiated with the lemmas in list order. Each lemma's root partition and element processing are the
-    loop_root/loop_element functions of its bundle part (generate_bundle_part), linked by the device-link step,
+    loop_root/loop_elements functions of its bundle part (generate_bundle_part), linked by the device-link step,
     so this unit compiles in seconds."""
     for L in lemmas:
         if L.numtype == "f32":
@@ -788,10 +790,12 @@ def generate_bundle(name, lemmas):
     for ns in nss:
         out += ["namespace %s {" % ns,
                 "__device__ bool loop_root(const LoopArgs& la, unsigned& gen);",
-                "__device__ void loop_element(const LoopArgs& la, std::uint64_t e);",
+                "__device__ void loop_elements(const LoopArgs& la, std::uint64_t e0, std::uint64_t k);",
                 "struct M {",
                 "    __device__ static bool root(const LoopArgs& la, unsigned& gen) { return loop_root(la, gen); }",
-                "    __device__ static void element(const LoopArgs& la, std::uint64_t e) { loop_element(la, e); }",
+                "    __device__ static void elements(const LoopArgs& la, std::uint64_t e0, std::uint64_t k) {",
+                "        loop_elements(la, e0, k);",
+                "    }",
                 "};",
                 "} // namespace %s" % ns]
     out += ["static cudaError_t bundle_launch_%s(const BundleArgs& b, unsigned blocks, cudaStream_t s) {" % name,

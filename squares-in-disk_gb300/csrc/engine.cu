@@ -594,7 +594,24 @@ struct Lane {
     Lane& operator=(const Lane&) = delete;
     ~Lane() {
         if(st) cudaStreamSynchronize(st);
+        if(stage) cudaFreeHost(stage);
         if(own_stream && st) cudaStreamDestroy(st);
+    }
+
+    /// Pinned host copies of the device loop's small transfers (its request slot going in, its control words and
+    /// counters coming back), so that they are asynchronous and share one wait.
+    struct LoopStage {
+        ReqDev in, out;
+        LoopCtl ctl;
+    };
+    LoopStage* stage = nullptr;
+    LoopStage& loop_stage() {
+        if(!stage) {
+            void* p = nullptr;
+            cuda_check(cudaMallocHost(&p, sizeof(LoopStage)), "pinned loop staging");
+            stage = static_cast<LoopStage*>(p);
+        }
+        return *stage;
     }
 
     /// Node re-iteration settings (ProverSettings::max_iterations_per_node and the two criteria).
@@ -740,8 +757,15 @@ struct Lane {
             }
             cuda_check(cudaMemsetAsync(r->qdepth.p, 0, std::size_t(r->nboxes), st), "sub-box depth");
         }
+        if(root_on_device) {
+            // the loop's own read-back gives the counts; no wait here (the staging copy is pinned, and the loop's
+            // read-back waits for the stream before the stage is written again)
+            LoopStage& sg = loop_stage();
+            sg.in = h;
+            cuda_check(cudaMemcpyAsync(req_dev.p + slot, &sg.in, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
+            return;
+        }
         cuda_check(cudaMemcpyAsync(req_dev.p + slot, &h, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
-        if(root_on_device) return;   // the loop's own read-back gives the counts; no wait here
         cuda_check(cudaStreamSynchronize(st), "request slot");
         if(r->full && !r->resume && !root_on_device) {
             root_part_index = r->part_index;
@@ -764,6 +788,8 @@ struct Lane {
     DevBuf<float2> lb_pbox;
     DevBuf<float4> lb_psplit;
     DevBuf<unsigned long long> lb_ctl;
+    DevBuf<std::uint8_t> lb_hull_depth;
+    static constexpr int kLoopGroupMax = 128;                   // elements a block takes at once, at most
 
     static constexpr std::uint64_t kBlockListItems = 2048;       // items of one per-block list
     static constexpr std::uint64_t kBlockEscChildren = 1 << 14;  // children per float-pass chunk of a block
@@ -814,8 +840,11 @@ struct Lane {
             la.dl_box[d] = l.box.p; la.dl_depth[d] = l.depth.p; la.dl_tag[d] = l.tag.p; la.dl_cap[d] = l.cap;
             p_cap = std::max(p_cap, l.cap);
         }
-        // per-block lists of one element's levels
-        std::uint64_t bp_cap = 1, items = 1;
+        // elements a block takes at once: enough for about one child per thread on the first static level (or the
+        // re-split's first level); the per-block lists of their levels
+        const int nsub0 = S > 0 ? int(stat[0].subdivisions) : int(dyn[0].subdivisions);
+        la.group_max = std::uint32_t(std::max(1, std::min(kLoopGroupMax, 128 / std::max(nsub0, 1))));
+        std::uint64_t bp_cap = 1, items = la.group_max;
         for(int j = 1; j < S; ++j) {
             items = std::min(items * std::uint64_t(stat[std::size_t(j - 1)].subdivisions), kBlockListItems);
             lb_sbox[j].reserve(std::size_t(G) * items * std::uint64_t(n));
@@ -824,7 +853,7 @@ struct Lane {
             la.bs_box[j] = lb_sbox[j].p; la.bs_elem[j] = lb_selem[j].p; la.bs_path[j] = lb_spath[j].p; la.bs_cap[j] = items;
             bp_cap = std::max(bp_cap, items);
         }
-        items = 1;
+        items = la.group_max;
         for(int d = 1; d < D; ++d) {
             items = std::min(items * std::uint64_t(dyn[std::size_t(d - 1)].subdivisions), kBlockListItems);
             lb_dbox[d].reserve(std::size_t(G) * items * std::uint64_t(n));
@@ -832,9 +861,11 @@ struct Lane {
             la.bd_box[d] = lb_dbox[d].p; la.bd_depth[d] = lb_ddepth[d].p; la.bd_cap[d] = items;
             bp_cap = std::max(bp_cap, items);
         }
-        lb_hull.reserve(std::size_t(G) * std::uint64_t(n));
+        lb_hull.reserve(std::size_t(G) * 2 * la.group_max * std::uint64_t(n));
+        lb_hull_depth.reserve(std::size_t(G) * 2 * la.group_max);
         lb_ctl.reserve(std::size_t(G) * kBlockCtlWords);
         la.b_hull_box = lb_hull.p;
+        la.b_hull_depth = lb_hull_depth.p;
         la.b_ctl = lb_ctl.p;
         if(fp32_first) {
             esc.reserve(kEscChunk);
@@ -857,11 +888,12 @@ struct Lane {
     /// kernel ran on, or which waits for it). Returns false if the proof's queue or a list would have overflowed
     /// (its counts are then incomplete; the caller redoes the proof on the host-driven loop).
     bool finish_loop(Request* r) {
-        LoopCtl c{};
-        ReqDev h{};
-        cuda_check(cudaMemcpyAsync(&c, loop_ctl.p, sizeof(LoopCtl), cudaMemcpyDeviceToHost, st), "loop control");
-        cuda_check(cudaMemcpyAsync(&h, req_dev.p + r->slot, sizeof(ReqDev), cudaMemcpyDeviceToHost, st), "request");
+        LoopStage& sg = loop_stage();
+        cuda_check(cudaMemcpyAsync(&sg.ctl, loop_ctl.p, sizeof(LoopCtl), cudaMemcpyDeviceToHost, st), "loop control");
+        cuda_check(cudaMemcpyAsync(&sg.out, req_dev.p + r->slot, sizeof(ReqDev), cudaMemcpyDeviceToHost, st), "request");
         cuda_check(cudaStreamSynchronize(st), "device proof loop");
+        const LoopCtl c = sg.ctl;
+        const ReqDev h = sg.out;
         if(c.error == kLoopTimeout) fail(SID_ERR_TIMEOUT, "device proof loop: a grid barrier gave up");
         // an append that did not fit is counted, not written
         if(c.error != kLoopOk || c.overflow != 0 || h.cnt[RC_OVERFLOW] != 0 || h.cnt[RC_QSIZE] != 0) return false;

@@ -74,7 +74,9 @@ struct LoopArgs {
     std::uint64_t bs_cap[kLoopMaxLevels];
     double2* bd_box[kLoopMaxLevels]; std::uint8_t* bd_depth[kLoopMaxLevels];
     std::uint64_t bd_cap[kLoopMaxLevels];
-    double2* b_hull_box;                   // nargs per block
+    std::uint32_t group_max;               // elements a block takes at once (at most)
+    double2* b_hull_box;                   // per block: two lists (final generation, re-split) of group_max hulls,
+    std::uint8_t* b_hull_depth;            // variable-major (box [v * group_max + j]), with their depths
     float2* b_pbox; float4* b_psplit; std::uint64_t b_p_cap;   // b_p_cap parents per block
     std::uint32_t* b_esc; std::uint64_t b_esc_cap;
     unsigned long long* b_ctl;             // kBlockCtlWords per block
@@ -207,17 +209,17 @@ template<class L, class T> __device__ __forceinline__ LevelArgs loop_args(const 
     return a;
 }
 
-/// Static levels of one element, run by one block (Lane::run_static on the block's lists): depth first, a level's
-/// input taken in chunks whose children fit the next list; the innermost level joins the element's hull
-/// (MODE_HULL) or stores criticals (MODE_CRIT). Level 0's one input item is in_box (stride in_stride), the
-/// element's box. Iterative (an explicit offset per level), so the kernel needs no call stack for it.
+/// Static levels of a group of elements, run by one block (Lane::run_static on the block's lists): depth first, a
+/// level's input taken in chunks whose children fit the next list; the innermost level joins each element's hull
+/// (MODE_HULL) or stores criticals (MODE_CRIT). Level 0's n0 input items are in_box (stride in_stride), item i
+/// being element elem + i. Iterative (an explicit offset per level), so the kernel needs no call stack for it.
 template<class L, class T> __device__ void block_static(const LoopArgs& la, const double2* in_box, std::uint64_t in_stride,
-                                                     std::uint32_t elem, int final_mode) {
+                                                     std::uint64_t n0, std::uint32_t elem, int final_mode) {
     const int n = la.nargs;
     const int S = la.n_stat;
     std::uint64_t off[kLoopMaxLevels], cnt_in[kLoopMaxLevels];
     off[0] = 0;
-    cnt_in[0] = 1;
+    cnt_in[0] = n0;
     int j = 0;
     while(j >= 0) {
         const LoopSplit& sp = la.stat[j];
@@ -235,7 +237,6 @@ template<class L, class T> __device__ void block_static(const LoopArgs& la, cons
             a.in_path = la.bs_path[j] + boff;
         }
         a.elem_tag = la.step_tag;
-        a.elem_base = elem;                // level 0: the item is the element itself
         a.var = sp.arg;
         a.nsub = sp.subdivisions;
         a.it_limit = n;
@@ -246,6 +247,7 @@ template<class L, class T> __device__ void block_static(const LoopArgs& la, cons
         if(last) {
             a.in_begin = 0;
             a.n_in = cnt_in[j];
+            a.elem_base = elem;            // level 0 only: item i is element elem + i
             a.hull_lo = la.hull;
             a.hull_hi = la.hull + la.step_cap * n;
             a.hull_zlo = la.hull + 2 * la.step_cap * n;
@@ -268,6 +270,7 @@ template<class L, class T> __device__ void block_static(const LoopArgs& la, cons
         __syncthreads();
         a.in_begin = off[j];
         a.n_in = cnt_in[j] - off[j] < chunk ? cnt_in[j] - off[j] : chunk;
+        a.elem_base = elem + std::uint32_t(off[j]);   // level 0: item in_begin + i is element elem + in_begin + i
         a.out_box = la.bs_box[j + 1] + boff * std::uint64_t(n);
         a.out_stride = cap;
         a.out_cap = cap;
@@ -286,15 +289,15 @@ template<class L, class T> __device__ void block_static(const LoopArgs& la, cons
     }
 }
 
-/// Dynamic re-split of one box (an element's hull, in_box with stride in_stride, its depth at *in_depth) with
+/// Dynamic re-split of n0 boxes (elements' hulls, in_box with stride in_stride, their depths in_depth[i]) with
 /// depth + 1, run by one block depth first like block_static; the last level appends to the request's queue.
 template<class L, class T> __device__ void block_dynamic(const LoopArgs& la, const double2* in_box, std::uint64_t in_stride,
-                                                      const std::uint8_t* in_depth) {
+                                                      const std::uint8_t* in_depth, std::uint64_t n0) {
     const int n = la.nargs;
     const int D = la.n_dyn;
     std::uint64_t off[kLoopMaxLevels], cnt_in[kLoopMaxLevels];
     off[0] = 0;
-    cnt_in[0] = 1;
+    cnt_in[0] = n0;
     int d = 0;
     while(d >= 0) {
         const LoopSplit& sp = la.dyn[d];
@@ -356,66 +359,95 @@ template<class L, class T> __device__ void block_dynamic(const LoopArgs& la, con
     }
 }
 
-/// One queue element (step item e), by one block: static recursion with hull join, then the hull's final
-/// generation or re-split. Lemmas without static splits: the element is its own only leaf and hull.
-template<class L, class T> __device__ void block_element(const LoopArgs& la, std::uint64_t e) {
+/// Elements a block takes at once in a step that takes `take` elements of a proof on `blocks` blocks: one each while
+/// that leaves blocks idle, more while the elements outnumber the blocks, up to la.group_max (enough to give the
+/// first static level about one child per thread). Uniform over the grid.
+__device__ __forceinline__ std::uint64_t loop_group(const LoopArgs& la, std::uint64_t take, std::uint64_t blocks) {
+    const std::uint64_t k = take / blocks;
+    return k < 1 ? 1 : (k > la.group_max ? la.group_max : k);
+}
+
+/// Queue elements e0 .. e0 + k - 1 of the step list (k <= group_max), by one block: static recursion with hull
+/// join, then each non-empty hull's final generation or re-split, the hulls of the group together. Lemmas without
+/// static splits: every element is its own only leaf and hull.
+template<class L, class T> __device__ void block_elements(const LoopArgs& la, std::uint64_t e0, std::uint64_t k) {
     constexpr int N = L::NARGS;
     ReqDev* r = la.req + la.tag;
-    double2* hb = la.b_hull_box + std::uint64_t(blockIdx.x) * N;
-    __shared__ int nonempty;
-    if(la.n_stat == 0) {
-        if(threadIdx.x == 0) {
-            atomicAdd(&r->cnt[RC_LEAVES], 1ull);
-            for(int v = 0; v < N; ++v) hb[v] = la.step_box[std::uint64_t(v) * la.step_cap + e];
-            nonempty = 1;
-        }
-    } else {
-        for(int k = int(threadIdx.x); k < N; k += int(blockDim.x)) {
-            la.hull[e * N + k] = ~0ull;
-            la.hull[la.step_cap * N + e * N + k] = 0ull;
-            la.hull[2 * la.step_cap * N + e * N + k] = ~0ull;
-            la.hull[3 * la.step_cap * N + e * N + k] = ~0ull;
+    const std::uint64_t G = la.group_max;
+    double2* fbox = la.b_hull_box + std::uint64_t(blockIdx.x) * 2 * G * N;    // final generation
+    double2* rbox = fbox + G * N;                                             // re-split
+    std::uint8_t* fdep = la.b_hull_depth + std::uint64_t(blockIdx.x) * 2 * G;
+    std::uint8_t* rdep = fdep + G;
+    __shared__ unsigned nfin, nres;
+    if(threadIdx.x == 0) {
+        nfin = 0;
+        nres = 0;
+    }
+    if(la.n_stat > 0) {
+        for(std::uint64_t t = threadIdx.x; t < k * N; t += blockDim.x) {
+            const std::uint64_t w = e0 * N + t;
+            la.hull[w] = ~0ull;
+            la.hull[la.step_cap * N + w] = 0ull;
+            la.hull[2 * la.step_cap * N + w] = ~0ull;
+            la.hull[3 * la.step_cap * N + w] = ~0ull;
         }
         __syncthreads();
-        // level 0's one item is the element: its column of the step list
-        block_static<L, T>(la, la.step_box + e, la.step_cap, std::uint32_t(e), MODE_HULL);
-        // decode the hull (k_hull_finalize): min of lower bounds, max of upper bounds, zeros signed as the first
-        if(threadIdx.x == 0) {
-            nonempty = loop_read(&la.hull[e * N]) != ~0ull;
-            if(nonempty) {
-                for(int v = 0; v < N; ++v) {
-                    double lo = key_value(loop_read(&la.hull[e * N + v]));
-                    double hi = key_value(loop_read(&la.hull[la.step_cap * N + e * N + v]));
-                    if(lo == 0.0) lo = (loop_read(&la.hull[2 * la.step_cap * N + e * N + v]) & 1ull) ? -0.0 : 0.0;
-                    if(hi == 0.0) hi = (loop_read(&la.hull[3 * la.step_cap * N + e * N + v]) & 1ull) ? -0.0 : 0.0;
-                    hb[v] = make_double2(lo, hi);
-                }
+        // level 0's items are the elements: their columns of the step list
+        block_static<L, T>(la, la.step_box + e0, la.step_cap, k, std::uint32_t(e0), MODE_HULL);
+    } else {
+        __syncthreads();
+    }
+    // each element's hull (k_hull_finalize): min of lower bounds, max of upper bounds, zeros signed as the first
+    // leaf's; non-empty hulls go to the final-generation or the re-split list of the block
+    for(std::uint64_t j = threadIdx.x; j < k; j += blockDim.x) {
+        const std::uint64_t e = e0 + j;
+        bool nonempty = true;
+        if(la.n_stat > 0) nonempty = loop_read(&la.hull[e * N]) != ~0ull;
+        else atomicAdd(&r->cnt[RC_LEAVES], 1ull);
+        if(!nonempty) continue;
+        const std::uint8_t depth = la.step_depth[e];
+        const bool fin = depth >= r->generations;
+        const unsigned slot = atomicAdd(fin ? &nfin : &nres, 1u);
+        double2* out = fin ? fbox : rbox;
+        if(fin) fdep[slot] = depth;
+        else rdep[slot] = depth;
+        for(int v = 0; v < N; ++v) {
+            double2 h;
+            if(la.n_stat > 0) {
+                double lo = key_value(loop_read(&la.hull[e * N + v]));
+                double hi = key_value(loop_read(&la.hull[la.step_cap * N + e * N + v]));
+                if(lo == 0.0) lo = (loop_read(&la.hull[2 * la.step_cap * N + e * N + v]) & 1ull) ? -0.0 : 0.0;
+                if(hi == 0.0) hi = (loop_read(&la.hull[3 * la.step_cap * N + e * N + v]) & 1ull) ? -0.0 : 0.0;
+                h = make_double2(lo, hi);
+            } else {
+                h = la.step_box[std::uint64_t(v) * la.step_cap + e];
             }
+            out[std::uint64_t(v) * G + slot] = h;
         }
     }
     __syncthreads();
-    const int ok = nonempty;
-    __syncthreads();                      // every thread has read the flag before the next element rewrites it
-    if(!ok) return;
-    const std::uint8_t depth = la.step_depth[e];
-    if(depth >= r->generations) {
+    const unsigned nf = nfin, nr = nres;
+    __syncthreads();                      // every thread has read the counts before the next group resets them
+    if(nf > 0) {
         if(la.n_stat == 0) {
-            if(threadIdx.x == 0) {
+            // the hulls are the leaves: each a leaf and a critical
+            for(std::uint64_t j = threadIdx.x; j < nf; j += blockDim.x) {
                 atomicAdd(&r->cnt[RC_LEAVES], 1ull);
                 const unsigned long long slot = atomicAdd(&r->cnt[RC_CRITICALS], 1ull);
                 if(slot < r->crit_cap) {
                     for(int v = 0; v < N; ++v) {
-                        r->crit[(slot * N + v) * 2] = hb[v].x;
-                        r->crit[(slot * N + v) * 2 + 1] = hb[v].y;
+                        const double2 h = fbox[std::uint64_t(v) * G + j];
+                        r->crit[(slot * N + v) * 2] = h.x;
+                        r->crit[(slot * N + v) * 2 + 1] = h.y;
                     }
                 }
             }
+            __syncthreads();
         } else {
-            block_static<L, T>(la, hb, 1, std::uint32_t(e), MODE_CRIT);
+            block_static<L, T>(la, fbox, G, nf, 0u, MODE_CRIT);
         }
-    } else {
-        block_dynamic<L, T>(la, hb, 1, la.step_depth + e);
     }
+    if(nr > 0) block_dynamic<L, T>(la, rbox, G, rdep, nr);
     __syncthreads();
 }
 
@@ -550,7 +582,12 @@ template<class L, class T> __global__ void __launch_bounds__(128, SID_LOOP_MIN_B
         // popped: children append from here (a queue append reserves its slot atomically from this size)
         if(blockIdx.x == 0 && threadIdx.x == 0) r->cnt[RC_QSIZE] = begin;
         if(!loop_barrier(la.sync, gen)) return;
-        for(std::uint64_t e = blockIdx.x; e < take; e += gridDim.x) block_element<L, T>(la, e);
+        const std::uint64_t k = loop_group(la, take, gridDim.x);
+        const std::uint64_t units = (take + k - 1) / k;
+        for(std::uint64_t u = blockIdx.x; u < units; u += gridDim.x) {
+            const std::uint64_t e0 = u * k;
+            block_elements<L, T>(la, e0, take - e0 < k ? take - e0 : k);
+        }
         if(!loop_barrier(la.sync, gen)) return;
     }
 }
@@ -588,7 +625,7 @@ struct BundleArgs {
 static_assert(sizeof(BundleArgs) <= 32000, "bundle arguments must fit the kernel parameter space");
 
 // Each member type M of a bundle kernel gives its lemma's root partition and element processing as
-// M::root(la, gen) and M::element(la, e): grid_root_partition<L, double> and block_element<L, double> of the
+// M::root(la, gen) and M::elements(la, e0, k): grid_root_partition<L, double> and block_elements<L, double> of the
 // lemma, compiled in the lemma's own translation unit with separate compilation (csrc/codegen.py), so the bundle
 // kernel's own unit stays small.
 template<int I, class L0, class... Ls> __device__ bool bundle_roots(const BundleArgs& b, unsigned& gen) {
@@ -600,11 +637,12 @@ template<int I, class L0, class... Ls> __device__ bool bundle_roots(const Bundle
     }
 }
 
-template<int I, class L0, class... Ls> __device__ void bundle_element(const BundleArgs& b, int i, std::uint64_t e) {
+template<int I, class L0, class... Ls>
+__device__ void bundle_elements(const BundleArgs& b, int i, std::uint64_t e0, std::uint64_t k) {
     if(i == I) {
-        L0::element(b.p[I], e);
+        L0::elements(b.p[I], e0, k);
     } else {
-        if constexpr(sizeof...(Ls) > 0) bundle_element<I + 1, Ls...>(b, i, e);
+        if constexpr(sizeof...(Ls) > 0) bundle_elements<I + 1, Ls...>(b, i, e0, k);
     }
 }
 
@@ -651,6 +689,14 @@ template<class... Ls> __global__ void __launch_bounds__(128, SID_LOOP_MIN_BLOCKS
         }
         const std::uint64_t total = first[kBundleMax];
         if(total == 0) break;
+        // work units: groups of elements of one proof (loop_group, sized by the whole step's elements)
+        std::uint64_t ufirst[kBundleMax + 1], group[kBundleMax];
+        ufirst[0] = 0;
+        for(int i = 0; i < kBundleMax; ++i) {
+            const std::uint64_t take = first[i + 1] - first[i];
+            group[i] = i < b.n ? loop_group(b.p[i], total, gridDim.x) : 1;
+            ufirst[i + 1] = ufirst[i] + (take + group[i] - 1) / group[i];
+        }
         for(int i = 0; i < b.n; ++i) {
             const std::uint64_t take = first[i + 1] - first[i];
             if(take == 0) continue;
@@ -665,10 +711,12 @@ template<class... Ls> __global__ void __launch_bounds__(128, SID_LOOP_MIN_BLOCKS
             }
         }
         if(!loop_barrier(sync, gen)) return;
-        for(std::uint64_t g = blockIdx.x; g < total; g += gridDim.x) {
+        for(std::uint64_t u = blockIdx.x; u < ufirst[kBundleMax]; u += gridDim.x) {
             int i = 0;
-            while(g >= first[i + 1]) ++i;
-            bundle_element<0, Ls...>(b, i, g - first[i]);
+            while(u >= ufirst[i + 1]) ++i;
+            const std::uint64_t e0 = (u - ufirst[i]) * group[i];
+            const std::uint64_t take = first[i + 1] - first[i];
+            bundle_elements<0, Ls...>(b, i, e0, take - e0 < group[i] ? take - e0 : group[i]);
         }
         if(!loop_barrier(sync, gen)) return;
     }

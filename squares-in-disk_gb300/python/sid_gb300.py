@@ -605,6 +605,8 @@ def main(argv=None):
     """Command line: prove a lemma once or more on GPU 0 and print the counts.
 
       python sid_gb300.py prove <lemma> [--precision 0|1|2] [--noprop MASK] [--repeat N] [--generations G]
+                                [--device-loop BLOCKS]
+      python sid_gb300.py bundle <lemma> <lemma> ... [--precision 0|1|2] [--repeat N] [--blocks BLOCKS]
       python sid_gb300.py describe <lemma> [--root]
     """
     import argparse
@@ -617,6 +619,13 @@ def main(argv=None):
     p.add_argument("--generations", type=int, default=8)
     p.add_argument("--noprop", type=lambda v: int(v, 0), default=None,
                    help="float-pass levels without propagation (default: all)")
+    p.add_argument("--device-loop", type=int, default=0,
+                   help="prove in one persistent kernel on this many blocks (default: host-driven levels)")
+    b = sub.add_parser("bundle", help="prove several lemmas together in one persistent kernel")
+    b.add_argument("lemmas", nargs="+")
+    b.add_argument("--precision", type=int, default=PRECISION_PLAIN)
+    b.add_argument("--repeat", type=int, default=1)
+    b.add_argument("--blocks", type=int, default=0, help="grid size (default: every block that can be resident)")
     q = sub.add_parser("describe", help="print a compiled lemma's arguments, bounds and constraints")
     q.add_argument("lemma")
     q.add_argument("--root", action="store_true", help="add the initial runtime range (needs the GPU engine)")
@@ -631,9 +640,17 @@ def main(argv=None):
         print(describe_ir(ir, root), end="")
         return 0
     eng = Engine(0)
+    if args.cmd == "bundle":
+        ids = [eng.register(lemma_ir(n)) for n in args.lemmas]
+        for _ in range(args.repeat):
+            for n, r in zip(args.lemmas, eng.prove_bundle(ids, precision=args.precision, blocks=args.blocks)):
+                print(n, "precision", args.precision, r, flush=True)
+        eng.close()
+        return 0
     lid = eng.register(lemma_ir(args.lemma))
     for _ in range(args.repeat):
-        r = eng.prove(lid, generations=args.generations, precision=args.precision, fp32_noprop_mask=args.noprop)
+        r = eng.prove(lid, generations=args.generations, precision=args.precision, fp32_noprop_mask=args.noprop,
+                      device_loop=args.device_loop)
         print(args.lemma, "precision", args.precision, r, flush=True)
     eng.close()
     return 0
