@@ -405,6 +405,24 @@ __device__ __forceinline__ unsigned long long reserve_queue_slots(unsigned activ
     return slot;
 }
 
+/// Replace box[var] by child c of its split into nsub pieces. The variable is known only at run time; a switch per
+/// variable keeps every index into the box a constant. (Selecting it inside an unrolled loop over the variables,
+/// `if(v == var) box[v] = ...`, let the compiler merge the stores into one store at a computed index, which put
+/// the whole box of the level kernels in local memory.)
+template<int V, int N, class T> __device__ __forceinline__ void split_box(Iv<T>* box, int var, int nsub, int c) {
+    if constexpr(V < N) {
+        switch(var) {
+            case V: {
+                T lo, hi;
+                split_child(box[V].lo, box[V].hi, nsub, c, lo, hi);
+                box[V] = {lo, hi, false};
+                return;
+            }
+            default: split_box<V + 1, N, T>(box, var, nsub, c);
+        }
+    }
+}
+
 /// Child c of item `item` in T: split the item's variable (splitter.hpp:44-59), propagate, test the
 /// level's rows. Returns whether the child survives; `box` is its propagated box. float_rows (double
 /// only): the rows are first tested in float on the propagated box rounded outward. Every float interval
@@ -421,12 +439,8 @@ __device__ __forceinline__ bool eval_child(const LevelArgs& a, const std::uint64
     for(int v = 0; v < N; ++v) {
         double2 b = a.in_box[std::uint64_t(v) * a.in_stride + item];
         box[v] = {T(b.x), T(b.y), false};
-        if(v == a.var) {
-            T lo, hi;
-            split_child(box[v].lo, box[v].hi, a.nsub, c, lo, hi);
-            box[v] = {lo, hi, false};
-        }
     }
+    split_box<0, N, T>(box, a.var, a.nsub, c);
     bool ok = !propagate<L, T>(a.var, box, a.it_limit, a.rec_limit);
     if(ok && a.row_end > a.row_begin) {
         if constexpr(sizeof(T) == sizeof(double)) {
@@ -705,6 +719,16 @@ __device__ __forceinline__ void filter_result_block(const LevelArgs& a, bool val
     }
 }
 
+/// The float box of child c in place of box[var] (the parent's float range), dispatched per variable as split_box.
+template<int V, int N> __device__ __forceinline__ void split_box_f32(Iv<float>* box, int var, float4 sp, int nsub, int c) {
+    if constexpr(V < N) {
+        switch(var) {
+            case V: split_child_f32(box[V].lo, box[V].hi, sp, nsub, c, box[V].lo, box[V].hi); return;
+            default: split_box_f32<V + 1, N>(box, var, sp, nsub, c);
+        }
+    }
+}
+
 /// Float pass over block `vb` of a chunk's children (all 128 threads of the executing block call it).
 template<class L> __device__ __forceinline__ void filter_f32_vblock(const LevelArgs& a, std::uint64_t vb) {
     constexpr int N = L::NARGS;
@@ -724,8 +748,8 @@ template<class L> __device__ __forceinline__ void filter_f32_vblock(const LevelA
         for(int v = 0; v < N; ++v) {
             const float2 f = a.pbox[std::uint64_t(v) * a.pstride + j];
             box[v] = {f.x, f.y, false};
-            if(v == a.var) split_child_f32(f.x, f.y, a.psplit[j], a.nsub, c, box[v].lo, box[v].hi);
         }
+        split_box_f32<0, N>(box, a.var, a.psplit[j], a.nsub, c);
         ok = a.fp32_noprop || !propagate<L, float>(a.var, box, a.it_limit, a.rec_limit);
         if(ok && a.row_end > a.row_begin) ok = L::template rows_ok<float>(a.row_begin, a.row_end, box);
         tag = item_tag(a, item);

@@ -123,3 +123,17 @@ def test_bench_batch_2e24_bit_exact(engine, oracle):
         check_operands(engine, oracle, ir, lid, np.ascontiguousarray(glo[:, s][:, keep]),
                        np.ascontiguousarray(ghi[:, s][:, keep]))
     assert verdicts.min() > 0, verdicts
+
+
+@pytest.mark.parametrize("name", ["top_packing_2", "one_subcontainer", "two_subcontainer", "four_subcontainer"])
+def test_large_ragged_batch_equals_the_all_double_kernel(engine, name):
+    """A ragged batch just above 2^22 cuboids (a partial last block, deferred cuboids from many blocks) gives the
+    all-double kernel's boxes and verdicts bit for bit, for lemmas of 2 to 4 variables."""
+    ir = sid.lemma_ir(name)
+    n = sid.ir_nargs(ir)
+    lid = engine.register(ir)
+    lo, hi = sid.synthetic_batch(engine.root_box(lid, n), (1 << 22) + 12345, seed=SEED + 7)
+    glo, ghi, gv = device_batch(engine, lid, lo, hi)
+    plo, phi, pv = device_batch(engine, lid, lo, hi, plain=True)
+    assert np.array_equal(gv, pv) and same_bits(glo, plo) and same_bits(ghi, phi)
+    assert len(np.unique(gv)) >= 2           # the batch exercises more than one verdict
