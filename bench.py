@@ -286,6 +286,50 @@ def serve_stream(eng, sid, precision, rates=SERVE_RATES, n_syn=SERVE_SYNTHETIC):
     return out
 
 
+def serve_lanes(eng, sid, precision, rate=1000.0, n_syn=SERVE_SYNTHETIC, widths=(1, 2, 4, 8, 11)):
+    """How the served form's latency scales with the number of lemmas served at once: synthetic sub-box requests
+    only (bench.py's distribution), Poisson arrivals at `rate`, the lemma drawn uniformly from the first k lemmas
+    of the set (one lane each, all lanes warmed up first), for each k in `widths`: p50/p99 time to verdict and
+    cuboids/s."""
+    names = sid.lemma_names()
+    lids = {n: eng.register(sid.lemma_ir(n)) for n in names}
+    roots = {n: eng.root_box(lids[n], sid.ir_nargs(sid.lemma_ir(n))) for n in names}
+    out = {}
+    with sid.Server(eng, precision=precision) as srv:
+        for n in names:
+            rid = srv.submit(lids[n], sid.synthetic_request(roots[n], np.random.default_rng(1), k=1))
+            srv.wait(rid)
+            srv.release(rid)
+        for k in widths:
+            use = names[:k]
+            rng = np.random.default_rng(SERVE_SEED + k)
+            syn = []
+            for _ in range(n_syn):
+                n = use[int(rng.integers(len(use)))]
+                syn.append((n, sid.synthetic_request(roots[n], rng)))
+            gaps = rng.exponential(1.0 / rate, n_syn)
+            t0 = time.perf_counter()
+            ids = []
+            t_next = t0
+            for (n, boxes), g in zip(syn, gaps):
+                t_next += g
+                delay = t_next - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ids.append(srv.submit(lids[n], boxes))
+            res = [srv.wait(rid) for rid in ids]
+            wall = time.perf_counter() - t0
+            for rid in ids:
+                srv.release(rid)
+            lat = [r["seconds_to_verdict"] for r in res]
+            cub = sum(r["cuboids"] for r in res)
+            out["lemmas_%d" % k] = {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99), "cuboids": cub,
+                                    "cuboids_per_s": cub / wall, "all_proved": all(r["state"] == sid.REQ_DONE for r in res)}
+    out["workload"] = ("%d synthetic sub-box requests per width at %g requests/s over the first k lemmas "
+                       "(one lane each)" % (n_syn, rate))
+    return out
+
+
 BATCHED_LEMMAS = ("four_subcontainer", "five_subcontainer", "six_subcontainer", "seven_subcontainer")
 
 
@@ -515,7 +559,8 @@ def run_ours(args):
     if not args.no_serve:
         serve = {"fp32": serve_stream(eng, sid, PRECISION_FP32), "plain": serve_stream(eng, sid, PRECISION_PLAIN),
                  "workload": "whole lemma set + %d seeded synthetic sub-box requests per rate, Poisson arrivals"
-                             % SERVE_SYNTHETIC}
+                             % SERVE_SYNTHETIC,
+                 "lanes_fp32": serve_lanes(eng, sid, PRECISION_FP32)}
 
     if rank != 0:
         return 0

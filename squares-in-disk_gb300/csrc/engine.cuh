@@ -823,10 +823,15 @@ template<class L, class H> __global__ void __launch_bounds__(128, SID_FILTER_MIN
 template<class L, int MODE> __device__ __forceinline__ void level_esc_grid(const LevelArgs& a) {
     const std::uint64_t n = *reinterpret_cast<volatile unsigned long long*>(a.esc_count);
     const std::uint64_t stride = std::uint64_t(gridDim.x) * blockDim.x;
+    // few escalated children (the float pass refuted nearly all): 2 to 32 lanes each, so that they spread over
+    // more warps and each warp runs only its own children's paths (lane_shift_for)
+    const std::uint32_t sh = lane_shift_for(n, stride);
+    const std::uint64_t nv = n << sh;
     // warp-uniform rounds: every lane of a warp takes part in each of its warp's rounds
-    for(std::uint64_t base = std::uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
-        const std::uint64_t j = base + lane_id();
-        const bool valid = j < n;
+    for(std::uint64_t base = std::uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < nv; base += stride) {
+        const std::uint64_t v = base + lane_id();
+        const std::uint64_t j = v >> sh;
+        const bool valid = (v & ((std::uint64_t(1) << sh) - 1u)) == 0 && j < n;
         std::uint64_t item = 0;
         int c = 0;
         if(valid) {

@@ -24,6 +24,13 @@ def test_oracle_matches_published_counts(oracle, name):
     assert r["criticals"] == 0 and r["repeated"] == 0
 
 
+def test_oracle_four_subcontainer_published_counts(oracle):
+    """The Four Subcontainer Lemma (37.2 M cuboids, ~20 s on 8 threads) against its published counts."""
+    r = oracle.prove(sid.lemma_ir("four_subcontainer"))
+    assert [r["cuboids"], r["leaves"]] == PUBLISHED["four_subcontainer"]
+    assert r["criticals"] == 0
+
+
 @pytest.mark.parametrize("variant", ["f64", "f32"])
 def test_oracle_expected_criticals(oracle, variant):
     r = oracle.prove(sid.lemma_ir("expected_critical_" + variant), generations=2, max_criticals=1000)
