@@ -1431,7 +1431,7 @@ void eval_batch_ordered(sid_engine* eng, Lemma* lem, const double* lo, const dou
     const bool defers = batch_defers(nargs);
     if(defers) {
         eng->batch_slow.reserve(std::size_t(n));
-        eng->batch_slow_count.reserve(1);
+        eng->batch_slow_count.reserve(2);   // one counter per kind of deferred cuboid
         a.slow = eng->batch_slow.p;
         a.slow_count = eng->batch_slow_count.p;
     }

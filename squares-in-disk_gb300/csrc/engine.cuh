@@ -885,7 +885,8 @@ struct BatchArgs {
     unsigned long long* double_rows;   // if set: += cuboids whose constraints float could not refute
     // deferred cuboids (both set, or neither): the evaluation kernel lists the cuboids whose propagation
     // reaches one of L::SLOW_BOUNDS or whose constraints float cannot refute, and k_eval_batch_slow
-    // evaluates them on full warps; slow holds up to n cuboid indices, *slow_count is cleared per launch
+    // evaluates them on full warps; slow holds up to n cuboid indices (the two kinds from either end),
+    // slow_count[0..1] are cleared per launch
     std::uint64_t* slow;
     unsigned long long* slow_count;
     unsigned slow_blocks;         // grid of k_eval_batch_slow: the device's SMs x 8 resident blocks (0: 1216)
@@ -908,15 +909,18 @@ constexpr int kInlineLanes = 8;
 __host__ __device__ constexpr bool batch_inline(int nargs) { return nargs <= 2; }
 
 /// Appends the indices of the lanes with `want` to the batch's deferred list (one atomic per warp). Every
-/// lane of the warp calls it.
-__device__ __forceinline__ void defer_cuboids(const BatchArgs& a, bool want, std::uint64_t i) {
+/// lane of the warp calls it. The list holds two kinds apart, so that k_eval_batch_slow runs each kind on warps of
+/// its own: kind 0 (the propagation reached a slow bound) fills it from the front, counted in slow_count[0];
+/// kind 1 (float could not refute the constraints, so they are tested in double) from the back, in slow_count[1].
+__device__ __forceinline__ void defer_cuboids(const BatchArgs& a, bool want, std::uint64_t i, int kind) {
     const unsigned m = __ballot_sync(0xffffffffu, want);
     if(!m) return;
     const int leader = __ffs(m) - 1;
     unsigned long long base = 0;
-    if(int(lane_id()) == leader) base = atomicAdd(a.slow_count, (unsigned long long)__popc(m));
+    if(int(lane_id()) == leader) base = atomicAdd(a.slow_count + kind, (unsigned long long)__popc(m));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if(want) a.slow[base + __popc(m & lanes_below())] = i;
+    const unsigned long long slot = base + __popc(m & lanes_below());
+    if(want) a.slow[kind == 0 ? slot : a.n - 1 - slot] = i;
 }
 
 /// Resident 128-thread blocks per SM the batch kernel is compiled for: 10 (48 registers) for lemmas with at
@@ -994,7 +998,7 @@ template<class L, class T, bool DEFER> __device__ __forceinline__ void batch_res
             }
             defer = false;
         }
-        defer_cuboids(a, defer, i);
+        defer_cuboids(a, defer, i, 1);
     }
 }
 
@@ -1099,7 +1103,7 @@ template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, ba
             for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
         }
         batch_stage1<L, T, DEFER>(a, valid, i, box, push, defer);
-        if constexpr(DEFER) defer_cuboids(a, defer, i);
+        if constexpr(DEFER) defer_cuboids(a, defer, i, 0);
         const unsigned m = __ballot_sync(0xffffffffu, push);
         if(m) {
             int at = 0;
@@ -1127,19 +1131,25 @@ template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, ba
     }
 }
 
-/// The deferred cuboids of a batch (BatchArgs::slow, *slow_count of them), one per thread on full warps:
+#ifndef SID_SLOW_MIN_BLOCKS
+#define SID_SLOW_MIN_BLOCKS 8       // resident 128-thread blocks per SM the deferred-work kernel is compiled for
+#endif
+
+/// The deferred cuboids of a batch (BatchArgs::slow: slow_count[0] of kind 0 from the front, slow_count[1] of kind 1
+/// from the back), one per thread on full warps, each kind on warps of its own (but the one warp where they meet):
 /// each is evaluated from its input box exactly as the first and second stage of k_eval_batch would have
 /// (propagation with every bound, the comparison-only constraints in double, the others in float and in
 /// double where float does not refute), so its outputs are those of the undeferred evaluation bit for bit.
-template<class L, class T> __global__ void __launch_bounds__(128, 8) k_eval_batch_slow(const BatchArgs a) {
+template<class L, class T> __global__ void __launch_bounds__(128, SID_SLOW_MIN_BLOCKS) k_eval_batch_slow(const BatchArgs a) {
     constexpr int N = L::NARGS;
-    const std::uint64_t n = *a.slow_count;
+    const std::uint64_t n0 = a.slow_count[0];
+    const std::uint64_t n = n0 + a.slow_count[1];
     const std::uint64_t st = a.stride ? a.stride : a.n;
     const bool rest = L::has_rest(N - 1, N);
     unsigned long long n_double = 0;
     for(std::uint64_t j = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n;
         j += std::uint64_t(gridDim.x) * blockDim.x) {
-        const std::uint64_t i = a.slow[j];
+        const std::uint64_t i = j < n0 ? a.slow[j] : a.slow[a.n - 1 - (j - n0)];
         Iv<T> box[N];
         #pragma unroll
         for(int v = 0; v < N; ++v) box[v] = {T(a.lo[std::uint64_t(v) * st + i]), T(a.hi[std::uint64_t(v) * st + i]), false};
@@ -1316,7 +1326,7 @@ template<class L, class T> cudaError_t launch_eval_batch(const BatchArgs& a, cud
     const std::uint64_t blocks = (a.n + per_block - 1) / per_block;
     if constexpr(batch_defers(L::NARGS)) {
         if(a.slow) {
-            const cudaError_t e = cudaMemsetAsync(a.slow_count, 0, sizeof(unsigned long long), s);
+            const cudaError_t e = cudaMemsetAsync(a.slow_count, 0, 2 * sizeof(unsigned long long), s);
             if(e != cudaSuccess) return e;
             k_eval_batch<L, T, true><<<unsigned(blocks), threads, 0, s>>>(a);
             // grid-stride over the deferred list, whose length only the device knows: enough blocks to fill
