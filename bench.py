@@ -44,8 +44,8 @@ BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
 # DRAM bytes (read + write) of one evaluation on this workload (k_eval_batch and k_eval_batch_slow), from an ncu
 # capture of the same kernels on the same batch (dram__bytes_read.sum + dram__bytes_write.sum); traffic grows in
 # proportion to the batch
-NCU_TRAFFIC_BYTES_2E24 = 0.824258e9 + 0.781132e9 + 0.045890e9 + 0.008301e9
-NCU_FP64_PIPE_ACTIVE = 0.630
+NCU_TRAFFIC_BYTES_2E24 = 0.824222e9 + 0.780581e9 + 0.044808e9 + 0.007536e9
+NCU_FP64_PIPE_ACTIVE = 0.628
 # FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
 FP64_LANES_PER_CLOCK = 304
 # FP32 lanes per clock of the whole GPU: 152 SMs x 128
