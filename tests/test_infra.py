@@ -41,6 +41,34 @@ def test_codegen_runs_on_all_ir(tmp_path):
     assert (tmp_path / "registry.cu").exists()
 
 
+def test_codegen_writes_bundles(tmp_path):
+    """Bundles (bundles.txt beside the IRs): one kernel unit per bundle that calls each lemma's separately compiled
+    proof-loop parts, one part unit per bundled lemma, the bundle in the registry; float lemmas and unknown names
+    are rejected."""
+    irs = [os.path.join(sid.LEMMA_DIR, f) for f in os.listdir(sid.LEMMA_DIR) if f.endswith(".sidir")]
+    irs += [os.path.join(sid.KAT_DIR, f) for f in os.listdir(sid.KAT_DIR) if f.endswith(".sidir")]
+    bundles = [os.path.join(sid.LEMMA_DIR, "bundles.txt"), os.path.join(sid.KAT_DIR, "bundles.txt")]
+    cmd = [sys.executable, os.path.join(sid.PKG, "csrc", "codegen.py"), "--out", str(tmp_path)]
+    subprocess.run(cmd + [x for b in bundles for x in ("--bundles", b)] + irs, check=True, stdout=subprocess.DEVNULL)
+    unit = (tmp_path / "bundle_subcontainers_4to7.cu").read_text()
+    assert "launch_proof_loop_bundle<lemma_four_subcontainer::M, lemma_five_subcontainer::M, " \
+           "lemma_six_subcontainer::M, lemma_seven_subcontainer::M>" in unit
+    for n in ("four_subcontainer", "five_subcontainer", "six_subcontainer", "seven_subcontainer",
+              "expected_critical_f64", "expected_critical2_f64"):
+        part = (tmp_path / ("bpart_lemma_%s.cu" % n)).read_text()
+        assert "#define SID_LEMMA_DEFS_ONLY" in part and "loop_elements" in part
+    reg = (tmp_path / "registry.cu").read_text()
+    assert "&bundle_subcontainers_4to7," in reg and "kNumBundles = 2;" in reg
+    # the lemma unit included by a part keeps its host launch table out of the part
+    lemma = (tmp_path / "lemma_four_subcontainer.cu").read_text()
+    assert lemma.count("#ifndef SID_LEMMA_DEFS_ONLY") == 2
+    bad = tmp_path / "bad.txt"
+    for line in ("f32: expected_critical_f32", "ghost: no_such_lemma", "too_many: a b c d e"):
+        bad.write_text(line + "\n")
+        r = subprocess.run(cmd + ["--bundles", str(bad)] + irs, capture_output=True, text=True)
+        assert r.returncode != 0, line
+
+
 def test_slow_bounds_are_the_costly_bound_functions():
     """The batch kernel defers cuboids whose propagation reaches a slow bound. One Subcontainer's slow bounds
     are 7 and 10 (a square root, and two square roots with a division); a bound that only copies a
