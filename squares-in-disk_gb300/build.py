@@ -87,7 +87,7 @@ def build(ir_files=None, extra_ir_dirs=(), verbose=False, jobs=None):
         os.remove(stale)
     part_deps = {p: [os.path.join(GEN, os.path.basename(p)[len("bpart_"):])] for p in parts}
     unit_flags = {u: ["-rdc=true"] for u in wanted_bundles}
-    unit_flags.update({u: ["-rdc=true", "-maxrregcount=128"] for u in parts})
+    unit_flags.update({u: ["-rdc=true", "-maxrregcount=%d" % _loop_register_cap()] for u in parts})
     units = sorted(parts) + gen_units + sorted(wanted_bundles) + [os.path.join(GEN, "registry.cu"),
                                                                   os.path.join(CSRC, "engine.cu"),
                                                                   os.path.join(CSRC, "noalloc.cu")]
@@ -136,6 +136,17 @@ def build(ir_files=None, extra_ir_dirs=(), verbose=False, jobs=None):
         with open(lib_stamp, "w") as f:
             f.write(link_stamp)
     return LIB
+
+
+def _loop_register_cap():
+    """Registers per thread of the proof-loop kernels: the bundle kernel is compiled for SID_LOOP_MIN_BLOCKS resident
+    128-thread blocks per SM (4 unless a tuning build defines it), and the separately compiled parts it calls must
+    not use more (65,536 registers per SM, allocated in groups of 8)."""
+    blocks = 4
+    for d in NVCC_FLAGS:
+        if d.startswith("-DSID_LOOP_MIN_BLOCKS="):
+            blocks = int(d.split("=", 1)[1])
+    return min(255, 65536 // (128 * max(blocks, 1))) // 8 * 8
 
 
 def _ns(path):

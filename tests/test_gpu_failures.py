@@ -130,3 +130,35 @@ def test_budget_below_one_request_still_serves_one_at_a_time(engine):
         res = [srv.wait(rid, 120000) for rid in ids]
     for st in res:
         assert st["state"] == sid.REQ_DONE and counts(st) == PUBLISHED["six_subcontainer"]
+
+
+BATCHED = ["four_subcontainer", "five_subcontainer", "six_subcontainer", "seven_subcontainer"]
+
+
+@pytest.mark.parametrize("kind,status", [(sid.INJECT_ALLOC, NOMEM), (sid.INJECT_LAUNCH, CUDA)])
+def test_device_loop_and_bundle_report_injected_failures_and_recover(engine, kind, status):
+    """A failure while a one-kernel proof or a bundle is set up or launched reaches the caller as its status; the
+    cached lanes then prove correctly again, in the loop and in the bundle."""
+    ids = [engine.register(sid.lemma_ir(n)) for n in BATCHED]
+    six = ids[2]
+    failed = 0
+    for countdown in (1, 2, 3, 5, 8, 13):
+        sid.inject_failure(kind, countdown)
+        try:
+            got = engine.prove_bundle(ids, precision=sid.PRECISION_FP32, blocks=152)
+            assert [counts(g) for g in got] == [PUBLISHED[n] for n in BATCHED]
+        except sid.SidError as e:
+            failed += 1
+            assert e.status == status, str(e)
+        sid.inject_failure(kind, 0)
+        sid.inject_failure(kind, countdown)
+        try:
+            assert counts(engine.prove(six, precision=sid.PRECISION_FP32, device_loop=152)) == PUBLISHED[BATCHED[2]]
+        except sid.SidError as e:
+            failed += 1
+            assert e.status == status, str(e)
+        sid.inject_failure(kind, 0)
+    assert failed > 0
+    got = engine.prove_bundle(ids, precision=sid.PRECISION_FP32)
+    assert [counts(g) for g in got] == [PUBLISHED[n] for n in BATCHED]
+    assert counts(engine.prove(six, precision=sid.PRECISION_FP32, device_loop=152)) == PUBLISHED[BATCHED[2]]
