@@ -598,10 +598,14 @@ template<class L, class T> cudaError_t launch_proof_loop(const LoopArgs& la, uns
                                        0, s);
 }
 
-/// Resident 128-thread blocks per SM of the proof loop (the cooperative grid's limit per SM).
+/// Resident 128-thread blocks per SM of the proof loop (the cooperative grid's limit per SM), asked of the runtime
+/// once per process: the query costs host time inside every short proof otherwise.
 template<class L, class T> int proof_loop_occupancy() {
+    static int cached = -1;
+    if(cached >= 0) return cached;
     int n = 0;
     if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_proof_loop<L, T>, 128, 0) != cudaSuccess) return 0;
+    cached = n;
     return n;
 }
 
@@ -730,8 +734,11 @@ template<class... Ls> cudaError_t launch_proof_loop_bundle(const BundleArgs& b, 
 }
 
 template<class... Ls> int proof_loop_bundle_occupancy() {
+    static int cached = -1;
+    if(cached >= 0) return cached;
     int n = 0;
     if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_proof_loop_bundle<Ls...>, 128, 0) != cudaSuccess) return 0;
+    cached = n;
     return n;
 }
 
