@@ -44,8 +44,8 @@ BYTES_PER_CUBOID = lambda nargs: 32 * nargs + 1  # noqa: E731
 # DRAM bytes (read + write) of one evaluation on this workload (k_eval_batch and k_eval_batch_slow), from an ncu
 # capture of the same kernels on the same batch (dram__bytes_read.sum + dram__bytes_write.sum); traffic grows in
 # proportion to the batch
-NCU_TRAFFIC_BYTES_2E24 = 0.824222e9 + 0.780581e9 + 0.044808e9 + 0.007536e9
-NCU_FP64_PIPE_ACTIVE = 0.628
+NCU_TRAFFIC_BYTES_2E24 = 0.826578e9 + 0.802608e9 + 0.044931e9 + 0.007485e9
+NCU_FP64_PIPE_ACTIVE = 0.649
 # FP64 lanes per clock of the whole GPU (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained)
 FP64_LANES_PER_CLOCK = 304
 # FP32 lanes per clock of the whole GPU: 152 SMs x 128
@@ -583,8 +583,8 @@ def run_ours(args):
                      "kernel": "k_eval_batch + k_eval_batch_slow (one_subcontainer, two stages, deferred cuboids, adaptive order)",
                      "kernel_ms": kernel_s * 1000.0, "ordering_ms_per_step": order_ms / max(prof_calls, 1),
                      "note": "algorithmic bytes (97 per cuboid) over the event-timed evaluation (both kernels); "
-                             "DRAM traffic is 2 % above them (the deferred kernel re-reads its cuboids); the "
-                             "main kernel's FP64 pipe is 63 % busy with comparisons and conversions (no double "
+                             "DRAM traffic is 3 % above them (the deferred kernel re-reads its cuboids); the "
+                             "main kernel's FP64 pipe is 65 % busy with comparisons and conversions (no double "
                              "arithmetic), it issues on 55 % of cycles and DRAM is 57 % busy (ncu)"},
         "gpu_launches": launches,
         "clocks": clk,

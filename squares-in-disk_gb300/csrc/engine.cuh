@@ -923,16 +923,25 @@ __device__ __forceinline__ void defer_cuboids(const BatchArgs& a, bool want, std
     if(want) a.slow[kind == 0 ? slot : a.n - 1 - slot] = i;
 }
 
-/// Resident 128-thread blocks per SM the batch kernel is compiled for: 10 (48 registers) for lemmas with at
-/// most 3 variables, where the added warps hide more latency than the spills cost (One Subcontainer, 2^24
-/// cuboids, with deferred work: 8 blocks 0.507 ms, 9 0.507, 10 0.496, 12 0.540, 14 and 16 0.560), 8 (64
-/// registers) above (Two Subcontainer, 2^22 cuboids: 0.170 ms at 8, 0.180 at 10; >= 5 subcontainers 3-4 %
-/// slower at 10). SID_BATCH_MIN_BLOCKS overrides it for tuning builds.
+/// Resident 128-thread blocks per SM the batch kernel is compiled for, and its 128-cuboid tiles per block: 12 blocks
+/// (40 registers) of 3 tiles for lemmas with at most 3 variables, where the added warps hide more latency than the
+/// spills cost (One Subcontainer, 2^24 cuboids, with the deferred cuboids in two lists by kind: 10 blocks of 4 tiles
+/// 0.415 ms, 12 of 4 0.410, 11 of 3 0.403, 12 of 3 0.402-0.403, 13 of 3 0.410, 12 of 2 0.417, 12 of 1 0.419, 14 and
+/// 16 of 4 0.431, 10 of 6 0.489, 8 of 4 0.453), 8 blocks (64 registers) of 4 tiles above (Two Subcontainer, 2^22
+/// cuboids: 0.170 ms at 8, 0.180 at 10; >= 5 subcontainers 3-4 % slower at 10). SID_BATCH_MIN_BLOCKS and
+/// SID_BATCH_TILES override them for tuning builds.
 template<class L> constexpr int batch_min_blocks() {
 #ifdef SID_BATCH_MIN_BLOCKS
     return SID_BATCH_MIN_BLOCKS;
 #else
-    return L::NARGS <= 3 ? 10 : 8;
+    return L::NARGS <= 3 ? 12 : 8;
+#endif
+}
+template<class L> __host__ __device__ constexpr int batch_tiles() {
+#ifdef SID_BATCH_TILES
+    return SID_BATCH_TILES;
+#else
+    return L::NARGS <= 3 ? 3 : 4;
 #endif
 }
 
@@ -941,10 +950,6 @@ template<class L> constexpr int batch_min_blocks() {
 template<class L, class T> __device__ __noinline__ bool rows_ok_outlined(int r0, int r1, const Iv<T>* box) {
     return L::template rows_ok<T>(r0, r1, box);
 }
-
-#ifndef SID_BATCH_TILES
-#define SID_BATCH_TILES 4           // 128-cuboid tiles per block of the batch kernel (1-16 measured, 4 fastest)
-#endif
 
 /// The second stage of the batch kernel for queue entry j (all lanes call it; `valid` marks the lanes with
 /// an entry): the cuboid's propagated box, which the first stage wrote, rounded outward to float; the
@@ -1064,7 +1069,7 @@ template<class L, class T, bool DEFER> __device__ __forceinline__ void batch_sta
 
 /// Leaf evaluation of independent cuboids: propagate after a change of the last variable
 /// (it_limit = nargs, rec_limit = 4) and test all constraints; the verdict is the double one bit for bit.
-/// Two stages per block of SID_BATCH_TILES tiles of 128 cuboids: (1) one thread per cuboid loads,
+/// Two stages per block of batch_tiles<L>() tiles of 128 cuboids: (1) one thread per cuboid loads,
 /// propagates, writes the propagated box and tests the constraints that only compare variables and
 /// constants, in the lemma's own type (exact, and for double lemmas cheaper than rounding the box to
 /// float: GB300 issues double comparisons and conversions alike on its narrow FP64 pipe); the cuboids that
@@ -1085,11 +1090,12 @@ template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, ba
     __shared__ std::uint32_t qpos[CAP];
     __shared__ int qn;
     const std::uint64_t st = a.stride ? a.stride : a.n;
-    const std::uint64_t first = std::uint64_t(blockIdx.x) * (128u * SID_BATCH_TILES);
+    constexpr int TILES = batch_tiles<L>();
+    const std::uint64_t first = std::uint64_t(blockIdx.x) * (128u * TILES);
     unsigned long long n_double = 0;
     if(threadIdx.x == 0) qn = 0;
     __syncthreads();
-    for(int tile = 0; tile < SID_BATCH_TILES; ++tile) {
+    for(int tile = 0; tile < TILES; ++tile) {
         const std::uint64_t base = first + std::uint64_t(tile) * 128u;
         if(base >= a.n) break;                                  // uniform over the block
         const std::uint64_t t = base + threadIdx.x;
@@ -1322,7 +1328,7 @@ template<class L, class T> cudaError_t launch_root_box(double2* out, cudaStream_
 template<class L, class T> cudaError_t launch_eval_batch(const BatchArgs& a, cudaStream_t s) {
     if(a.n == 0) return cudaSuccess;
     const unsigned threads = 128;
-    const std::uint64_t per_block = std::uint64_t(threads) * SID_BATCH_TILES;
+    const std::uint64_t per_block = std::uint64_t(threads) * batch_tiles<L>();
     const std::uint64_t blocks = (a.n + per_block - 1) / per_block;
     if constexpr(batch_defers(L::NARGS)) {
         if(a.slow) {
