@@ -1135,6 +1135,9 @@ template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, ba
         const unsigned long long w = __reduce_add_sync(0xffffffffu, unsigned(n_double));
         if(lane_id() == 0 && w) atomicAdd(a.double_rows, w);
     }
+    // the deferred-work kernel, launched as this grid's programmatic dependent, may be scheduled once every block
+    // got here (it waits for this grid's completion before it reads the list)
+    if constexpr(DEFER) asm volatile("griddepcontrol.launch_dependents;");
 }
 
 #ifndef SID_SLOW_MIN_BLOCKS
@@ -1148,6 +1151,9 @@ template<class L, class T, bool DEFER> __global__ void __launch_bounds__(128, ba
 /// double where float does not refute), so its outputs are those of the undeferred evaluation bit for bit.
 template<class L, class T> __global__ void __launch_bounds__(128, SID_SLOW_MIN_BLOCKS) k_eval_batch_slow(const BatchArgs a) {
     constexpr int N = L::NARGS;
+    // launched as the evaluation kernel's programmatic dependent: wait until that grid has completed and its
+    // writes (the list and its counters) are visible; a no-op for an ordinary launch
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const std::uint64_t n0 = a.slow_count[0];
     const std::uint64_t n = n0 + a.slow_count[1];
     const std::uint64_t st = a.stride ? a.stride : a.n;
@@ -1340,8 +1346,19 @@ template<class L, class T> cudaError_t launch_eval_batch(const BatchArgs& a, cud
             const std::uint64_t want_blocks = (a.n + threads - 1) / threads;
             const std::uint64_t fill = a.slow_blocks ? a.slow_blocks : 1216u;
             const std::uint64_t slow_blocks = want_blocks < fill ? want_blocks : fill;
-            k_eval_batch_slow<L, T><<<unsigned(slow_blocks), threads, 0, s>>>(a);
-            return cudaGetLastError();
+            // a programmatic dependent launch: its blocks are scheduled as the evaluation's last blocks finish
+            // instead of after the whole grid has drained
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(unsigned(slow_blocks));
+            cfg.blockDim = dim3(threads);
+            cfg.dynamicSmemBytes = 0;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            return cudaLaunchKernelEx(&cfg, k_eval_batch_slow<L, T>, a);
         }
     }
     k_eval_batch<L, T, false><<<unsigned(blocks), threads, 0, s>>>(a);
