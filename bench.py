@@ -54,6 +54,65 @@ OPS_TABLE = os.path.join(REPO, "tests", "golden", "ops_per_cuboid.json")
 CLOCK_WINDOW_S = 0.6   # seconds of load the clock sampler sees after the timed steps
 
 
+def gpu_host_numa(local_rank):
+    """The host NUMA node and CPUs next to this rank's GPU (sysfs of its PCI function, from the CUDA device's PCI
+    location), or (None, None) where the system does not say."""
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(local_rank)
+        dev = "/sys/bus/pci/devices/%04x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+        node = int(open(os.path.join(dev, "numa_node")).read().strip())
+        cpus = set()
+        for part in open(os.path.join(dev, "local_cpulist")).read().strip().split(","):
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+        return (node if node >= 0 else None), cpus
+    except Exception:
+        return None, None
+
+
+class NearHostMemory:
+    """Within the block, this process allocates host memory on the NUMA node next to the GPU and runs on that node's
+    CPUs where it may, so that pinned buffers (placed when first touched) are not behind the socket link: on a
+    two-socket Grace host a far node halves the host-device copy rate. Affinity and memory policy are restored
+    afterwards; both are settings of this process only."""
+    SYS_SET_MEMPOLICY = {"aarch64": 237, "x86_64": 238}
+    MPOL_DEFAULT, MPOL_PREFERRED = 0, 1
+
+    def __init__(self, local_rank):
+        self.node, self.cpus = gpu_host_numa(local_rank)
+        self.report = {"gpu_host_node": self.node}
+
+    def _mempolicy(self, mode, node):
+        import ctypes
+        import platform
+        nr = self.SYS_SET_MEMPOLICY.get(platform.machine())
+        if nr is None:
+            return False
+        libc = ctypes.CDLL(None, use_errno=True)
+        mask = ctypes.c_ulong(1 << node) if node is not None else None
+        ret = libc.syscall(nr, mode, ctypes.byref(mask) if mask is not None else None, 64 if mask is not None else 0)
+        return ret == 0
+
+    def __enter__(self):
+        self.old_cpus = os.sched_getaffinity(0)
+        if self.node is None:
+            return self
+        near = (self.cpus or set()) & self.old_cpus
+        if near:
+            os.sched_setaffinity(0, near)
+        self.report["cpus_near_gpu"] = len(near)
+        self.report["memory_policy"] = ("preferred node %d" % self.node
+                                        if self._mempolicy(self.MPOL_PREFERRED, self.node) else "default")
+        return self
+
+    def __exit__(self, *exc):
+        if self.node is not None:
+            self._mempolicy(self.MPOL_DEFAULT, None)
+        os.sched_setaffinity(0, self.old_cpus)
+        return False
+
+
 def measured_peaks():
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -521,27 +580,28 @@ def run_ours(args):
     # the all-double kernel (the reference's order, no float test) on the same batch: the FP64 baseline
     plain = plain_fp64_leg(eng, lid, d_lo, d_hi, o_lo, o_hi, o_v, n, nargs, stream, args)
 
-    # end to end through the C ABI with pinned host buffers
-    h_lo = torch.from_numpy(lo).pin_memory()
-    h_hi = torch.from_numpy(hi).pin_memory()
-    h_olo = torch.empty_like(h_lo).pin_memory()
-    h_ohi = torch.empty_like(h_hi).pin_memory()
-    h_v = torch.empty(n, dtype=torch.int8).pin_memory()
+    # end to end through the C ABI with pinned host buffers, allocated on the host memory next to the GPU
+    with NearHostMemory(local) as near:
+        h_lo = torch.from_numpy(lo).pin_memory()
+        h_hi = torch.from_numpy(hi).pin_memory()
+        h_olo = torch.empty_like(h_lo).pin_memory()
+        h_ohi = torch.empty_like(h_hi).pin_memory()
+        h_v = torch.empty(n, dtype=torch.int8).pin_memory()
 
-    def e2e_step():
-        sid._check(eng.L.sid_eval_batch(eng.h, lid, h_lo.data_ptr(), h_hi.data_ptr(), n, h_olo.data_ptr(),
-                                        h_ohi.data_ptr(), h_v.data_ptr()))
+        def e2e_step():
+            sid._check(eng.L.sid_eval_batch(eng.h, lid, h_lo.data_ptr(), h_hi.data_ptr(), n, h_olo.data_ptr(),
+                                            h_ohi.data_ptr(), h_v.data_ptr()))
 
-    e2e_step()
-    e2e_steps = max(3, args.steps // 2)
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
         e2e_step()
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(dist, e2e_s)
-    torch.cuda.synchronize()
+        e2e_steps = max(3, args.steps // 2)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_s = time.perf_counter() - t0
+        e2e_s = max_over_ranks(dist, e2e_s)
+        torch.cuda.synchronize()
     e2e_same = bool(np.array_equal(h_v.numpy(), o_v.cpu().numpy()) and
                     np.array_equal(h_olo.numpy().view(np.uint64), o_lo.cpu().numpy().view(np.uint64)) and
                     np.array_equal(h_ohi.numpy().view(np.uint64), o_hi.cpu().numpy().view(np.uint64)))
@@ -576,7 +636,7 @@ def run_ours(args):
                    "batch_per_gpu": n, "parallelism": "independent shards per GPU (no collective)",
                    "l2": "inputs 805 MB and outputs exceed the 129 MB L2; no flush"},
         "e2e": {"value": e2e_value, "unit": "cuboids/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps, "outputs_equal_device_path": e2e_same},
+                "steps": e2e_steps, "outputs_equal_device_path": e2e_same, "host_memory": near.report},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC_BYTES_2E24 * n / float(1 << 24), "peak_kind": peak_kind,
                      "fp64_pipe_active_ncu": NCU_FP64_PIPE_ACTIVE,
