@@ -179,7 +179,8 @@ int sid_fetch_criticals(sid_engine* engine, int lemma_id, double* out, uint64_t 
  * exceeds it skip the float pass and go straight to double) with a step size, and are timed by proving
  * the lemma, as long as max_seconds of proving allows. Every candidate must reproduce the first proof's
  * cuboid, leaf and critical counts or it is discarded. Proofs shorter than 5 ms also try the device proof loop
- * (sid_prove_opts.device_loop_blocks) on 38, 152 and 608 blocks. The fastest is stored with the lemma and used by
+ * (sid_prove_opts.device_loop_blocks) on 38, 152 and 608 blocks, with the chosen float-pass levels and with none
+ * (every level in the double kernel with float-first rows). The fastest is stored with the lemma and used by
  * SID_PRECISION_FP32_TUNED proofs and servers (servers drive their lanes from the host). */
 #define SID_MAX_LEVELS 16
 typedef struct sid_tuning {

@@ -2382,18 +2382,24 @@ int sid_lemma_autotune(sid_engine* engine, int lemma_id, double max_seconds, sid
                     t.step_elements = std::int64_t(step);
                 }
             }
-            // the device proof loop, for proofs short enough that launches and host reads dominate
+            // the device proof loop, for proofs short enough that launches and host reads dominate; there a level
+            // of a few hundred children may also be done sooner by the dense double kernel (float-first rows) than
+            // by the float pass and its two extra grid barriers, so the loop is also tried with no float pass
             if(t.seconds < kLoopTuneBelowSeconds) {
-                for(unsigned blocks : {38u, 152u, 608u}) {
-                    if(spent > max_seconds) break;
-                    sid_result r{};
-                    o.device_loop_blocks = blocks;
-                    timed(std::uint64_t(t.step_elements), t.fp32_level_mask, r);
-                    o.device_loop_blocks = 0;
-                    ++t.candidates;
-                    if(same(r) && r.seconds < t.seconds) {
-                        t.seconds = r.seconds;
-                        t.loop_blocks = blocks;
+                const std::uint32_t chosen = t.fp32_level_mask;
+                for(std::uint32_t mask : {chosen, 0u}) {
+                    for(unsigned blocks : {38u, 152u, 608u}) {
+                        if(spent > max_seconds) break;
+                        sid_result r{};
+                        o.device_loop_blocks = blocks;
+                        timed(std::uint64_t(t.step_elements), mask, r);
+                        o.device_loop_blocks = 0;
+                        ++t.candidates;
+                        if(same(r) && r.seconds < t.seconds) {
+                            t.seconds = r.seconds;
+                            t.loop_blocks = blocks;
+                            t.fp32_level_mask = mask;
+                        }
                     }
                 }
             }
