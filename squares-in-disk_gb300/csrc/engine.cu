@@ -413,8 +413,10 @@ __global__ void k_store_criticals(const double2* box, std::uint64_t stride, cons
 /// variable RD(lb), RU(lb), RD(w), RU(w), RU(ub) with w = (ub - lb) / nsub computed in double exactly as
 /// split_child does. One thread per parent, so the double work is paid once per parent, not per child.
 __global__ void k_parent_f32(const double2* in_box, std::uint64_t in_stride, std::uint64_t item0, std::uint64_t n_items,
-                             int nargs, int var, int nsub, float2* pbox, float4* psplit, std::uint64_t pstride) {
+                             int nargs, int var, int nsub, float2* pbox, float4* psplit, std::uint64_t pstride,
+                             unsigned long long* reset) {
     const std::uint64_t j = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if(j == 0 && reset) *reset = 0;   // the chunk's escalation count, which the float pass after this kernel fills
     if(j >= n_items) return;
     for(int v = 0; v < nargs; ++v) {
         const double2 b = in_box[std::uint64_t(v) * in_stride + item0 + j];
@@ -506,7 +508,6 @@ __global__ void k_order_scatter(const std::uint32_t* key, std::uint64_t n, std::
     order[atomicAdd(&offset[key[i]], 1u)] = std::uint32_t(i);
 }
 
-__global__ void k_add_counter(unsigned long long* dst, const unsigned long long* src) { *dst += *src; }
 
 struct GatherEntry {
     std::uint32_t slot;
@@ -1040,13 +1041,12 @@ struct Lane {
             psplit.reserve(n_items);
             k_parent_f32<<<unsigned((n_items + 127) / 128), 128, 0, st>>>(a.in_box, a.in_stride, a.in_begin + first,
                                                                           n_items, n, a.var, a.nsub, pbox.p, psplit.p,
-                                                                          n_items);
+                                                                          n_items, a.esc_count);
             cuda_check(cudaGetLastError(), "parent pass launch");
             a.pbox = pbox.p;
             a.psplit = psplit.p;
             a.pstride = n_items;
             a.pitem_begin = first;
-            cuda_check(cudaMemsetAsync(a.esc_count, 0, sizeof(unsigned long long), st), "reset escalation count");
             if(nval >= 0) {
                 hval.reserve(std::size_t(std::max(nval, 1)) * n_items);
                 hbits.reserve(n_items);
@@ -1057,7 +1057,7 @@ struct Lane {
             } else {
                 cuda_check(lem->k->filter_f32(a, st), "float pass launch");
             }
-            k_add_counter<<<1, 1, 0, st>>>(level_esc.p + level, a.esc_count);
+            a.esc_stat = level_esc.p + level;   // the double pass adds the chunk's escalations to the level's count
             const std::uint64_t want = (a.n_child + 127) / 128;
             const unsigned blocks = unsigned(std::min<std::uint64_t>(want, std::uint64_t(sm_count) * kEscBlocksPerSM));
             cuda_check(lem->k->level_esc(mode, a, blocks, st), "escalated pass launch");

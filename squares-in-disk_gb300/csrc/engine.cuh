@@ -307,6 +307,7 @@ struct LevelArgs {
     std::uint64_t child_begin, n_child;
     std::uint32_t* esc;
     unsigned long long* esc_count;
+    unsigned long long* esc_stat;     // if set, k_level_esc adds the list's length here (per-level statistics)
     // per-parent float data of the chunk (k_parent_f32): parents from item offset pitem_begin on
     const float2* pbox;               // pbox[v*pstride + j]; for the split variable (RD(lb), RU(ub))
     const float4* psplit;             // (RD(w), RU(lb), RU(w), 0) with w the double split width
@@ -822,6 +823,7 @@ template<class L, class H> __global__ void __launch_bounds__(128, SID_FILTER_MIN
 
 template<class L, int MODE> __device__ __forceinline__ void level_esc_grid(const LevelArgs& a) {
     const std::uint64_t n = *reinterpret_cast<volatile unsigned long long*>(a.esc_count);
+    if(a.esc_stat && blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(a.esc_stat, (unsigned long long)n);
     const std::uint64_t stride = std::uint64_t(gridDim.x) * blockDim.x;
     // few escalated children (the float pass refuted nearly all): 2 to 32 lanes each, so that they spread over
     // more warps and each warp runs only its own children's paths (lane_shift_for)
