@@ -604,6 +604,7 @@ struct Lane {
     struct LoopStage {
         ReqDev in, out;
         LoopCtl ctl;
+        unsigned long long words[8];     // counters read back between levels (read_counters)
     };
     LoopStage* stage = nullptr;
     LoopStage& loop_stage() {
@@ -650,14 +651,17 @@ struct Lane {
     const ReqDev& counters_of(const Request* r) const { return req_host[std::size_t(r->slot)]; }
     std::uint64_t queue_size(const Request* r) const { return counters_of(r).cnt[RC_QSIZE]; }
 
-    unsigned long long read_counter(unsigned long long* d) {
-        unsigned long long v = 0;
-        cuda_check(cudaMemcpyAsync(&v, d, sizeof(v), cudaMemcpyDeviceToHost, st), "read counter");
+    /// Read k adjacent device counters (one copy into pinned memory, one wait).
+    const unsigned long long* read_counters(const unsigned long long* d, int k) {
+        LoopStage& sg = loop_stage();
+        cuda_check(cudaMemcpyAsync(sg.words, d, sizeof(unsigned long long) * std::size_t(k), cudaMemcpyDeviceToHost, st),
+                   "read counter");
         cuda_check(cudaStreamSynchronize(st), "stream sync");
-        return v;
+        return sg.words;
     }
-    void set_counter(unsigned long long* d, unsigned long long v) {
-        cuda_check(cudaMemcpyAsync(d, &v, sizeof(v), cudaMemcpyHostToDevice, st), "set counter");
+    unsigned long long read_counter(const unsigned long long* d) { return read_counters(d, 1)[0]; }
+    void zero_counter(unsigned long long* d) {
+        cuda_check(cudaMemsetAsync(d, 0, sizeof(unsigned long long), st), "reset counter");
     }
 
     int free_slots() const {
@@ -1123,7 +1127,7 @@ struct Lane {
                 a.out_cap = out->cap;
                 a.out_depth = out->depth.p;
                 a.out_tag = out->tag.p;
-                set_counter(counters.p, 0);
+                zero_counter(counters.p);
                 launch(MODE_EMIT, a, int(d));
                 std::uint64_t cnt = read_counter(counters.p);
                 run_dynamic(d + 1, out->box.p, out->cap, out->depth.p, out->tag.p, 0, 0, cnt, initial, depth_add);
@@ -1171,7 +1175,7 @@ struct Lane {
             a.row_begin = sp.arg; a.row_end = row_end;
             a.out_box = out.box.p; a.out_stride = out.cap; a.out_cap = out.cap;
             a.out_elem = out.elem.p; a.out_path = out.path.p;
-            set_counter(counters.p, 0);
+            zero_counter(counters.p);
             launch(MODE_EMIT, a, int(dyn.size() + j));
             std::uint64_t cnt = read_counter(counters.p);
             run_static(j + 1, out.box.p, out.cap, out.elem.p, out.path.p, elem_tag, 0, cnt, final_mode);
@@ -1229,8 +1233,8 @@ struct Lane {
                                                             step.cap, step.depth.p, step.tag.p);
         cuda_check(cudaGetLastError(), "gather");
 
-        set_counter(counters.p + 1, 0);
-        set_counter(counters.p + 2, 0);
+        zero_counter(counters.p + 1);
+        zero_counter(counters.p + 2);
         if(stat.empty()) {
             const RouteIteration itr{max_iter, lem->k->is_f32, iter_single, iter_volume};
             k_route_elements<<<unsigned((B + 127) / 128), 128, 0, st>>>(
@@ -1274,7 +1278,7 @@ struct Lane {
                     BoxList& out = (in == &iter_in) ? iter_out : iter_in;
                     h.it_box = out.box.p; h.it_depth = out.depth.p; h.it_tag = out.tag.p; h.it_count = counters.p + 4;
                     h.it_stride = out.cap;
-                    set_counter(counters.p + 4, 0);
+                    zero_counter(counters.p + 4);
                 }
                 launch_gate("hull finalize");
                 k_hull_finalize<<<unsigned((n_elem + 127) / 128), 128, 0, st>>>(h);
@@ -1284,8 +1288,9 @@ struct Lane {
                 in = (in == &iter_in) ? &iter_out : &iter_in;
             }
         }
-        const std::uint64_t nfin = read_counter(counters.p + 1);
-        const std::uint64_t nnf = read_counter(counters.p + 2);
+        const unsigned long long* fin_nf = read_counters(counters.p + 1, 2);
+        const std::uint64_t nfin = fin_nf[0];
+        const std::uint64_t nnf = fin_nf[1];
         if(nfin > 0) {
             if(stat.empty()) {
                 k_store_criticals<<<unsigned((nfin + 127) / 128), 128, 0, st>>>(fin.box.p, step_cap, fin.tag.p, nfin, n,
