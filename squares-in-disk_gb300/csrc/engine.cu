@@ -596,6 +596,7 @@ struct Lane {
     ~Lane() {
         if(st) cudaStreamSynchronize(st);
         if(stage) cudaFreeHost(stage);
+        if(slots_pinned) cudaFreeHost(slots_pinned);
         if(own_stream && st) cudaStreamDestroy(st);
     }
 
@@ -770,7 +771,9 @@ struct Lane {
             cuda_check(cudaMemcpyAsync(req_dev.p + slot, &sg.in, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
             return;
         }
-        cuda_check(cudaMemcpyAsync(req_dev.p + slot, &h, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
+        LoopStage& sg = loop_stage();   // pinned; the wait below ends the copy before the stage is written again
+        sg.in = h;
+        cuda_check(cudaMemcpyAsync(req_dev.p + slot, &sg.in, sizeof(ReqDev), cudaMemcpyHostToDevice, st), "request slot");
         cuda_check(cudaStreamSynchronize(st), "request slot");
         if(r->full && !r->resume && !root_on_device) {
             root_part_index = r->part_index;
@@ -935,18 +938,27 @@ struct Lane {
     }
 
     /// Copy the counters of the used slots from the device table; checks the overflow flags.
+    /// Pinned host copy of the request table and the list-overflow flag, read back after every step.
+    ReqDev* slots_pinned = nullptr;
+    unsigned int* ovf_pinned = nullptr;
+
     void read_slots() {
         int hi = 0;
         for(int i = 0; i < max_slots; ++i) if(slot_req[std::size_t(i)]) hi = i + 1;
-        std::vector<ReqDev> tmp(std::size_t(std::max(hi, 1)));
-        unsigned int ovf = 0;
+        if(!slots_pinned) {
+            void* p = nullptr;
+            cuda_check(cudaMallocHost(&p, sizeof(ReqDev) * std::size_t(max_slots) + sizeof(ReqDev)), "pinned request table");
+            slots_pinned = static_cast<ReqDev*>(p);
+            ovf_pinned = reinterpret_cast<unsigned int*>(slots_pinned + max_slots);
+        }
+        const ReqDev* tmp = slots_pinned;
         if(hi > 0) {
-            cuda_check(cudaMemcpyAsync(tmp.data(), req_dev.p, sizeof(ReqDev) * std::size_t(hi), cudaMemcpyDeviceToHost, st),
+            cuda_check(cudaMemcpyAsync(slots_pinned, req_dev.p, sizeof(ReqDev) * std::size_t(hi), cudaMemcpyDeviceToHost, st),
                        "request table");
         }
-        cuda_check(cudaMemcpyAsync(&ovf, overflow.p, sizeof(ovf), cudaMemcpyDeviceToHost, st), "overflow flag");
+        cuda_check(cudaMemcpyAsync(ovf_pinned, overflow.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, st), "overflow flag");
         cuda_check(cudaStreamSynchronize(st), "request table sync");
-        if(ovf) fail(SID_ERR_CUDA, "internal error: a level list overflowed");
+        if(*ovf_pinned) fail(SID_ERR_CUDA, "internal error: a level list overflowed");
         for(int i = 0; i < hi; ++i) {
             if(!slot_req[std::size_t(i)]) continue;
             std::memcpy(req_host[std::size_t(i)].cnt, tmp[std::size_t(i)].cnt, sizeof(tmp[0].cnt));
